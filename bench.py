@@ -1,0 +1,368 @@
+#!/usr/bin/env python3
+"""Throughput of the voxel occlusion path in Grays/s (giga-rays per second).
+
+Workload (default "c2", the plain path at scale): 512^3 fine-voxel grid from
+seeded 3-octave value noise (threshold 0.55, frequency 1/32, ground slab y < 8)
+plus 2000 seeded boxes of 4-48 voxels per side; 1920x1080 primary-hit G-buffer
+(fp32 position, normal, roughness U[0.05,1]) from a seeded pinhole camera
+outside the grid; per pixel 1 shadow ray (maxt 100), 8 cosine-weighted AO rays
+(maxt 32) and 1 GGX specular-occlusion ray (maxt 256), all through the exact
+reference DDA (Light.frag:29-81). One step = one vxl_trace_occlusion call over
+the frame. Inputs are generated on the device and are not timed.
+
+Arms: default = libvxl CUDA path; --impl reference = the CPU restatement of
+the reference path (oracle/) on all host cores, over a bounded sample of the
+same frame per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "c2": dict(n=512, W=1920, H=1080, boxes=2000, n_shadow=1, n_ao=8, ao_len=32.0, n_spec=1, spec_len=256.0,
+               shadow_len=100.0, seed=2024),
+    "c1": dict(n=256, W=640, H=360, boxes=0, n_shadow=1, n_ao=4, ao_len=16.0, n_spec=0, spec_len=256.0,
+               shadow_len=100.0, seed=2024),
+}
+L2_BYTES = 129 * 1024 * 1024
+
+
+def camera(n):
+    # outside the grid (above and in front), looking at its centre
+    cam = np.array([0.5 * n, 1.15 * n, -0.1 * n], np.float32)
+    tgt = np.array([0.5 * n, 0.5 * n, 0.5 * n], np.float32)
+    return cam, tgt
+
+
+def light_dir(seed):
+    rng = np.random.default_rng(seed)
+    v = rng.normal(size=3)
+    v[1] = abs(v[1]) + 0.8  # above the horizon
+    return (v / np.linalg.norm(v)).astype(np.float32)
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.rows.append([c.strip() for c in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, name in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        return rank, world, local, dist
+    return 0, 1, 0, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# --------------------------------------------------------------- CPU oracle
+def cpu_sample_rays_per_s(g_r8, pos, nrm, rough, P, W, H, budget_s=12.0, threads=None):
+    """Time the oracle on whole image rows spread over the frame until about
+    budget_s of wall time; returns (rays/s, rows, seconds, threads)."""
+    import oracle
+
+    threads = threads or (os.cpu_count() or 1)
+    R = P.n_shadow + P.n_ao + P.n_spec
+    valid = (np.abs(nrm).reshape(-1, 3).sum(1) > 0).reshape(H, W)
+    order = np.random.default_rng(1).permutation(H)
+    rays = 0
+    rows = 0
+    t0 = time.perf_counter()
+    for y in order:
+        oracle.occlusion(g_r8, pos, nrm, rough, P, p0=int(y) * W, p1=int(y + 1) * W, threads=threads)
+        rays += int(valid[y].sum()) * R
+        rows += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return rays / dt, rows, dt, threads
+
+
+def run_reference(args, wl):
+    """--impl reference: the oracle port on the host cores (no GPU work)."""
+    import oracle
+
+    rank, world, local, dist = dist_setup(args)
+    if rank != 0:
+        return
+    n, W, H = wl["n"], wl["W"], wl["H"]
+    threads = os.cpu_count() or 1
+    g = oracle.scene_noise(n, n, n, seed=wl["seed"], threads=threads)
+    if wl["boxes"]:
+        oracle.scene_boxes(g, wl["seed"], wl["boxes"], 4, 48)
+    cam, tgt = camera(n)
+    pos, nrm, rough = oracle.gbuffer(g, cam, tgt, W, H, wl["seed"], threads=threads)
+    P = oracle.make_params(light_dir=light_dir(wl["seed"]), cam_pos=cam, bias=0.5, shadow_len=wl["shadow_len"],
+                           ao_len=wl["ao_len"], spec_len=wl["spec_len"], n_shadow=wl["n_shadow"], n_ao=wl["n_ao"],
+                           n_spec=wl["n_spec"], seed=wl["seed"])
+    per_step = []
+    for s in range(args.warmup + args.steps):
+        v, rows, dt, th = cpu_sample_rays_per_s(g, pos, nrm, rough, P, W, H, budget_s=args.ref_step_seconds,
+                                                threads=threads)
+        if s >= args.warmup:
+            per_step.append((v, rows, dt))
+    rays_s = sum(v * dt for v, _, dt in per_step) / sum(dt for _, _, dt in per_step)
+    val = rays_s / 1e9
+    R = wl["n_shadow"] + wl["n_ao"] + wl["n_spec"]
+    line = {
+        "impl": "reference", "metric": "Grays/s shadow+AO+spec occlusion (exact voxel DDA)", "value": val,
+        "unit": "Grays/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * statistics.mean(dt for _, _, dt in per_step), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": config_dict(wl),
+        "cpu_baseline": {"value": val, "unit": "Grays/s", "cores": threads, "kind": "port",
+                         "sample": "per step: whole image rows in seeded random order until %.0f s of wall time "
+                                   "(%d rows of %d on average), %d rays per pixel" % (
+                                       args.ref_step_seconds, statistics.mean(r for _, r, _ in per_step), H, R)},
+        "e2e": {"value": val, "unit": "Grays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def config_dict(wl):
+    return {"workload": "plain-%d^3-%dx%d-%dshadow+%dao(L%g)+%dspec" % (
+        wl["n"], wl["W"], wl["H"], wl["n_shadow"], wl["n_ao"], wl["ao_len"], wl["n_spec"]),
+        "grid": [wl["n"]] * 3, "image": [wl["W"], wl["H"]], "boxes": wl["boxes"],
+        "rays_per_pixel": wl["n_shadow"] + wl["n_ao"] + wl["n_spec"], "noise_threshold": 0.55,
+        "l2": "flushed between timed steps (256 MiB write outside the per-step events)"}
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_gpu(args, wl):
+    import torch
+
+    import voxelengine_gb300 as V
+
+    rank, world, local, dist = dist_setup(args)
+    torch.cuda.set_device(local)
+    V.build()
+    ctx = V.Context(local)
+    n, W, H = wl["n"], wl["W"], wl["H"]
+    npix = W * H
+    R = wl["n_shadow"] + wl["n_ao"] + wl["n_spec"]
+    G = V.Grid(ctx, n, n, n)
+    G.scene_noise(wl["seed"], 0.55, 1.0 / 32.0, 8)
+    if wl["boxes"]:
+        G.scene_boxes(wl["seed"], wl["boxes"], 4, 48)
+    cam, tgt = camera(n)
+    pos = torch.empty(npix * 3, dtype=torch.float32, device="cuda")
+    nrm = torch.empty_like(pos)
+    rough = torch.empty(npix, dtype=torch.float32, device="cuda")
+    V.scene_gbuffer(ctx, G, cam, tgt, W, H, wl["seed"], pos, nrm, rough)
+    P = V.make_params(light_dir=light_dir(wl["seed"]), cam_pos=cam, bias=0.5, shadow_len=wl["shadow_len"],
+                      ao_len=wl["ao_len"], spec_len=wl["spec_len"], n_shadow=wl["n_shadow"], n_ao=wl["n_ao"],
+                      n_spec=wl["n_spec"], seed=wl["seed"])
+    outs = {k: torch.empty(npix, dtype=torch.float32, device="cuda") for k in ("shadow", "ao", "ao_vis", "spec", "spec_t")}
+    valid = int((nrm.view(-1, 3).abs().sum(1) > 0).sum().item())
+    rays_per_step = valid * R
+
+    # per-ray fetch counts (S_ref) from one untimed pass with records
+    rec = torch.empty(npix * R * 6, dtype=torch.int32, device="cuda")
+    V.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, records=rec, **outs)
+    torch.cuda.synchronize()
+    steps_col = rec.view(-1, 6)[:, 4].view(npix, R)
+    vmask = (nrm.view(-1, 3).abs().sum(1) > 0)
+    s_ref = float(steps_col[vmask].double().mean().item())
+    hits = float(((rec.view(-1, 6)[:, 5] & 1).view(npix, R)[vmask]).double().mean().item())
+    del rec
+
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        V.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, **outs)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    l0 = ctx.launch_count()
+    with ClockSampler(local) as clk:
+        barrier(dist)
+        torch.cuda.synchronize()
+        for s in range(args.steps):
+            flush.fill_(float(s))
+            ev[s][0].record(stream)
+            V.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, **outs)
+            ev[s][1].record(stream)
+        torch.cuda.synchronize()
+        barrier(dist)
+    launches = ctx.launch_count() - l0
+    times = [a.elapsed_time(b) for a, b in ev]  # ms
+    t_total = max_over_ranks(dist, sum(times) / 1e3)
+    rays_total = sum_over_ranks(dist, rays_per_step * args.steps)
+    value = rays_total / t_total / 1e9
+
+    # end to end through the host-memory entry point (pinned buffers)
+    hp, hn, hr = pos.cpu().pin_memory(), nrm.cpu().pin_memory(), rough.cpu().pin_memory()
+    hout = {k: torch.empty(npix, dtype=torch.float32).pin_memory() for k in outs}
+    for _ in range(max(1, args.warmup)):
+        V.trace_occlusion_host(ctx, G, hp, hn, hr, npix, P, h_shadow=hout["shadow"], h_ao=hout["ao"],
+                               h_ao_vis=hout["ao_vis"], h_spec=hout["spec"], h_spec_t=hout["spec_t"])
+    torch.cuda.synchronize()
+    barrier(dist)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for s in range(args.steps):
+        V.trace_occlusion_host(ctx, G, hp, hn, hr, npix, P, h_shadow=hout["shadow"], h_ao=hout["ao"],
+                               h_ao_vis=hout["ao_vis"], h_spec=hout["spec"], h_spec_t=hout["spec_t"])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(dist)
+    t_e2e = max_over_ranks(dist, e0.elapsed_time(e1) / 1e3)
+    e2e = rays_total / t_e2e / 1e9
+    h2d = npix * (3 + 3 + 1) * 4
+    d2h = npix * 5 * 4
+
+    if rank != 0:
+        return
+    hbm, peak_kind = measured_peaks()
+    b_pix_in = 24 + (4 if wl["n_spec"] else 0)
+    b_pix_out = 4 * 5
+    b_ray = (b_pix_in + b_pix_out) / R + 4.0 * s_ref
+    ms = statistics.mean(times)
+    achieved = b_ray * rays_per_step / (ms / 1e3) / 1e9
+    line = {
+        "metric": "Grays/s shadow+AO+spec occlusion (exact voxel DDA)", "value": value, "unit": "Grays/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene and G-buffer)",
+        "config": config_dict(wl),
+        "rays_per_step": rays_per_step, "valid_pixels": valid, "s_ref_mean_fetches_per_ray": s_ref,
+        "hit_fraction": hits,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "peak_kind": peak_kind,
+                     "bytes_per_ray": b_ray,
+                     "note": "algorithmic bytes = ((28 B in + 20 B out) per pixel)/R + 4 B x S_ref per ray; "
+                             "per-launch time from CUDA events on the launch stream"},
+        "e2e": {"value": e2e, "unit": "Grays/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "path": "vxl_trace_occlusion_host, pinned host G-buffer and outputs"},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        g8 = torch.zeros((n // 2) ** 3, dtype=torch.uint8, device="cuda")
+        G.export_r8(g8)
+        torch.cuda.synchronize()
+        g_np = g8.cpu().numpy().reshape(n // 2, n // 2, n // 2)
+        import oracle
+
+        OP = oracle.make_params(light_dir=light_dir(wl["seed"]), cam_pos=cam, bias=0.5, shadow_len=wl["shadow_len"],
+                                ao_len=wl["ao_len"], spec_len=wl["spec_len"], n_shadow=wl["n_shadow"],
+                                n_ao=wl["n_ao"], n_spec=wl["n_spec"], seed=wl["seed"])
+        v, rows, dt, th = cpu_sample_rays_per_s(g_np, pos.cpu().numpy(), nrm.cpu().numpy(), rough.cpu().numpy(), OP,
+                                                W, H, budget_s=args.cpu_seconds)
+        line["cpu_baseline"] = {"value": v / 1e9, "unit": "Grays/s", "cores": th, "kind": "port",
+                                "sample": "%d whole image rows of %d in seeded random order (%.1f s), %d rays/px" % (
+                                    rows, H, dt, R)}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="vxl", choices=["vxl", "reference"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=4.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, wl)
+    else:
+        run_gpu(args, wl)
+
+
+if __name__ == "__main__":
+    main()

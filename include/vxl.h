@@ -1,0 +1,275 @@
+/*
+ * vxl.h — C ABI of libvxl, a GB300 (sm_103a) implementation of VoxelEngine's
+ * voxel-lighting path: the ShadowVox voxelizer and the voxel ray traversal
+ * behind raytraced shadows, ambient occlusion and specular occlusion.
+ *
+ * Conventions
+ *  - Every entry point returns vxl_status; nothing is thrown across the ABI.
+ *    vxl_last_error_string() gives a thread-local message for the last failure.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *    All device work is stream-ordered and asynchronous unless stated.
+ *  - Pointers documented as "device" are caller-owned device memory on the
+ *    context's GPU; "host" pointers are read before the call returns.
+ *  - Coordinates are in fine-voxel units: one unit is one ShadowVox bit,
+ *    0.1 world units (Sources/World/Systems/ShadowVoxSystem.cpp:147, x10).
+ *  - A grid of fine dimensions (nx,ny,nz) corresponds to the reference's R8
+ *    ShadowVox image of (nx/2, ny/2, nz/2) bytes, 2x2x2 voxels per byte.
+ */
+#ifndef VXL_H
+#define VXL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VXL_ABI_VERSION 1
+
+typedef enum vxl_status {
+    VXL_OK = 0,
+    VXL_ERR_INVALID_ARG = 1,
+    VXL_ERR_OOM = 2,
+    VXL_ERR_CUDA = 3,
+    VXL_ERR_TIMEOUT = 4,
+    VXL_ERR_OUT_OF_RANGE = 5,
+    VXL_ERR_IO = 6,
+    VXL_ERR_NOT_SUPPORTED = 7
+} vxl_status;
+
+typedef struct vxl_ctx vxl_ctx;
+typedef struct vxl_grid vxl_grid;
+
+/* ---------------------------------------------------------------- basics */
+int vxl_abi_version(void);
+const char* vxl_last_error_string(void);
+const char* vxl_status_string(vxl_status s);
+
+/* Context on one CUDA device. Owns library scratch buffers; one context per
+ * host thread, or guard it with a mutex. Replaces the engine's Graphics
+ * singleton for this path (Sources/Graphics/Graphics.h:23-32). */
+vxl_status vxl_ctx_create(int device, vxl_ctx** out);
+vxl_status vxl_ctx_destroy(vxl_ctx* ctx);
+/* number of kernels this library launched through ctx (diagnostics) */
+vxl_status vxl_ctx_launch_count(const vxl_ctx* ctx, uint64_t* out);
+
+/* ------------------------------------------------------------------ grid
+ * Replaces ShadowVoxSystem's R8Uint volume (ShadowVoxSystem.cpp:55-79,
+ * ShadowVoxSystem.h:29 GetVolumeImage). Storage: 1 bit per fine voxel in
+ * 4x4x4 bricks (one uint64 each), 8 bricks per 8^3 tile (64 bytes), tiles in
+ * x-fastest order, plus one zero tile of padding on the + side of every axis.
+ * nx, ny, nz must be even and in [2, 32768]. */
+typedef struct vxl_grid_desc {
+    int32_t nx, ny, nz;        /* fine dimensions */
+    int32_t tx, ty, tz;        /* tiles per axis, padding included */
+    uint64_t* words;           /* device: tx*ty*tz*8 uint64 */
+    size_t words_bytes;
+    uint32_t* tile_mask;       /* device: 1 bit per tile, "tile has any voxel set" */
+    size_t tile_mask_bytes;
+} vxl_grid_desc;
+
+vxl_status vxl_grid_create(vxl_ctx* ctx, int nx, int ny, int nz, vxl_grid** out);
+vxl_status vxl_grid_destroy(vxl_grid* grid);
+vxl_status vxl_grid_describe(const vxl_grid* grid, vxl_grid_desc* out);
+/* zero every voxel */
+vxl_status vxl_grid_clear(vxl_grid* grid, void* stream);
+/* rebuild the tile occupancy map after the words changed (the trace entry
+ * points read it); vxl_voxelize and the imports rebuild it themselves */
+vxl_status vxl_grid_build_bricks(vxl_grid* grid, void* stream);
+/* Reference layout in/out: device bytes [nz/2][ny/2][nx/2], byte x+y*sx+z*sx*sy,
+ * bit (x&1)|(y&1)<<1|(z&1)<<2 (ShadowVoxSystem.cpp:82-94, Light.frag:14-20). */
+vxl_status vxl_grid_import_r8(vxl_grid* grid, const uint8_t* d_bytes, void* stream);
+vxl_status vxl_grid_export_r8(const vxl_grid* grid, uint8_t* d_bytes, void* stream);
+/* Dense palette-index volume, device uint8 [nz][ny][nx]: voxel set where
+ * index >= opaque_min (16 in the reference: ShadowVoxSystem.cpp:145). */
+vxl_status vxl_grid_import_palette(vxl_grid* grid, const uint8_t* d_palette, int opaque_min, void* stream);
+/* number of set voxels (synchronous) */
+vxl_status vxl_grid_count(const vxl_grid* grid, uint64_t* out, void* stream);
+
+/* ------------------------------------------------------------- traversal */
+typedef enum vxl_mode {
+    VXL_MODE_DDA = 0,          /* raycastShadowVolume, Light.frag:29-81 (exact DDA) */
+    VXL_MODE_SPARSE = 1,       /* raycastShadowVolumeSparse, Light.frag:131-173 */
+    VXL_MODE_SUPERSPARSE = 2   /* raycastShadowVolumeSuperSparse, Light.frag:175-217 */
+} vxl_mode;
+
+/* per-ray result record (24 bytes) */
+typedef struct vxl_ray_record {
+    int32_t vx, vy, vz;  /* hit cell, or last cell tested on a miss */
+    float t;             /* DDA: best_t of the hit cell (Light.frag:57,62); marchers: returned distance */
+    int32_t steps;       /* occupancy fetches made */
+    int32_t flags;       /* VXL_RF_* */
+} vxl_ray_record;
+
+enum {
+    VXL_RF_HIT = 1,
+    VXL_RF_SELX = 2, VXL_RF_SELY = 4, VXL_RF_SELZ = 8, /* DDA axis select at the hit: normal = -sign(dir)*sel */
+    VXL_RF_EXIT_BOUNDS = 16,
+    VXL_RF_EXIT_STEPS = 32,
+    VXL_RF_EXIT_MAXT = 64,
+    VXL_RF_COARSE = 128
+};
+
+/* Trace n independent rays. Device rays float[n][7] = origin xyz, dir xyz,
+ * maxt (DDA) or dist (marchers). Device records[n]. Direct replacement for
+ * calls to raycastShadowVolume / ...Sparse / ...SuperSparse (Light.frag:29,131,175). */
+vxl_status vxl_trace_rays(vxl_ctx* ctx, const vxl_grid* grid, const float* d_rays, int64_t n, vxl_mode mode,
+                          vxl_ray_record* d_records, void* stream);
+
+/* G-buffer: device pointers, fine-voxel units. A pixel whose normal is
+ * (0,0,0) is sky: nothing is traced and its outputs are 1 (spec_t = spec_len). */
+typedef struct vxl_gbuffer {
+    const float* pos;    /* [npix][3] surface position */
+    const float* nrm;    /* [npix][3] unit surface normal */
+    const float* rough;  /* [npix] roughness, or NULL (then params.default_rough) */
+    int64_t npix;
+    int32_t width, height; /* informational; npix is authoritative */
+} vxl_gbuffer;
+
+/* DDA-mode ray generation (this library's definition; the reference's passes
+ * fire one jittered Sparse/SuperSparse ray each, see vxl_light_*):
+ *  origin  O = pos + nrm*bias
+ *  shadow  dir = light_dir, maxt = shadow_len                      -> shadow = hit ? 0 : 1
+ *  AO k    cosine-weighted (cosineSampleHemisphere, LightAmbient.frag:81-87) in the
+ *          tangent frame of LightAmbient.frag:112-113, u = PCG(seed, pixel, 64+2k / 65+2k),
+ *          maxt = ao_len -> ao = mean_k (min(t_k, ao_len)/ao_len)^2, ao_vis = mean_k miss
+ *  spec j  GGX half-vector (alpha = rough^2) about the normal, u = PCG(seed, pixel, 2j / 2j+1),
+ *          reflection of V = normalize(cam_pos - pos), maxt = spec_len
+ *          -> spec = mean_j miss, spec_t = mean_j (hit ? t : spec_len)
+ * Same layout as the oracle's params struct. */
+typedef struct vxl_trace_params {
+    float light_dir[3];   /* unit vector toward the light */
+    float cam_pos[3];     /* camera position (spec rays) */
+    float bias;           /* origin offset along the normal */
+    float shadow_len;     /* 100 in the reference's DDA call (LightAmbient.frag:163) */
+    float ao_len;
+    float spec_len;       /* 256 in the reference's DDA call (LightReflection.frag:104) */
+    float default_rough;
+    int32_t n_shadow;     /* 0 or 1 */
+    int32_t n_ao;         /* 0..64 */
+    int32_t n_spec;       /* 0..8 */
+    uint32_t seed;
+    int32_t mode;         /* VXL_MODE_DDA */
+} vxl_trace_params;
+
+/* Outputs: device float[npix] each, any may be NULL. records, if not NULL,
+ * is device vxl_ray_record[npix * (n_shadow + n_ao + n_spec)] in the order
+ * shadow, AO 0..n_ao-1, spec 0..n_spec-1 per pixel. */
+typedef struct vxl_outputs {
+    float* shadow;
+    float* ao;
+    float* ao_vis;
+    float* spec;
+    float* spec_t;
+    vxl_ray_record* records;
+} vxl_outputs;
+
+/* The drop-in for the traversal consumers of LightAmbientPipeline::Use /
+ * LightReflectionPipeline::Use (LightAmbientPipeline.h:35, LightReflectionPipeline.h:34):
+ * G-buffer and grid in, occlusion buffers out. */
+vxl_status vxl_trace_occlusion(vxl_ctx* ctx, const vxl_grid* grid, const vxl_gbuffer* gbuf,
+                               const vxl_trace_params* params, const vxl_outputs* out, void* stream);
+
+/* Same, with the G-buffer held in host memory (pinned or pageable): the
+ * library copies it in through its context staging buffers, traces, and
+ * copies the outputs back to host memory. Synchronous on `stream`. Host
+ * outputs may be NULL. */
+vxl_status vxl_trace_occlusion_host(vxl_ctx* ctx, const vxl_grid* grid, const float* h_pos, const float* h_nrm,
+                                    const float* h_rough, int64_t npix, const vxl_trace_params* params,
+                                    float* h_shadow, float* h_ao, float* h_ao_vis, float* h_spec, float* h_spec_t,
+                                    void* stream);
+
+/* ------------------------------------------------ reference light passes
+ * Bit-exact replacements for the live shader passes (Sparse/SuperSparse
+ * marchers with the reference's jitter). `noise` is the per-pixel blue-noise
+ * texel the shader reads with getNoise() (device float[npix][4]).
+ * records (optional) get one record per traced ray. */
+
+/* LightAmbient.frag:148-173. wcp = world position in fine units, i.e.
+ * (InverseView*pos).xyz*10 (:150); depth = linear depth (:136).
+ * Out: shadow (:167-169) and the ambient irradiance scalar d*d*0.05 (:121-125). */
+vxl_status vxl_light_ambient(vxl_ctx* ctx, const vxl_grid* grid, const float* d_wcp, const float* d_nrm,
+                             const float* d_depth, const float* d_noise, int64_t npix, float* d_shadow,
+                             float* d_irradiance, vxl_ray_record* d_records, void* stream);
+/* LightReflection.frag:92-113. view_r = (InverseView*vec4(R,0)).xyz before
+ * normalisation (:92). Out: t of raycastShadowVolumeSparse (256 = miss, :121). */
+vxl_status vxl_light_reflection(vxl_ctx* ctx, const vxl_grid* grid, const float* d_wcp, const float* d_nrm,
+                                const float* d_view_r, const float* d_rough, const float* d_noise, int64_t npix,
+                                float* d_t, vxl_ray_record* d_records, void* stream);
+/* LightPoint.frag:234-267 (spot = 0) / LightSpot.frag:83-117 (spot = 1).
+ * wpos in world units. Pixels beyond `range` are discarded (output untouched). */
+vxl_status vxl_light_point(vxl_ctx* ctx, const vxl_grid* grid, const float* d_wpos, const float* d_nrm,
+                           const float* d_noise, int64_t npix, const float light_pos[3], float range, int spot,
+                           float* d_shadow, vxl_ray_record* d_records, void* stream);
+
+/* ------------------------------------------------------------ voxelizer */
+typedef struct vxl_model {
+    const uint8_t* data;   /* device palette indices [sz][sy][sx] (VoxAsset::PixelAt, VoxAsset.h:52-56) */
+    int32_t sx, sy, sz;
+} vxl_model;
+
+typedef enum vxl_op { VXL_OP_CLEAR = 0, VXL_OP_SET = 1 } vxl_op;
+
+/* One placement: matrix = World * translate(-Pivot), column-major 4x4
+ * (ShadowVoxSystem.cpp:134-140). Every model voxel with index >= 16 maps to
+ * fine voxel ivec3((o + x*dx + y*dy + z*dz)*10), o = matrix[3], d* = matrix[0..2]*0.1,
+ * and is set or cleared there (ShadowVoxSystem.cpp:142-155, SetVolumeAt :82-94). */
+typedef struct vxl_instance {
+    float matrix[16];
+    int32_t model;
+    int32_t op;            /* vxl_op */
+} vxl_instance;
+
+/* Apply instances (host array) in array order: the result equals applying
+ * them one after another, as the reference's single-threaded loop does.
+ * aabb (optional, device int32[n][6]): per instance min xyz, max xyz of every
+ * mapped fine voxel, in or out of the grid, min/max-ed into the values the
+ * caller initialised it with (the reference starts them at (S-1,S-1,S-1) and
+ * (0,0,0), ShadowVoxSystem.cpp:128-132). Rebuilds the tile map. */
+vxl_status vxl_voxelize(vxl_ctx* ctx, vxl_grid* grid, const vxl_model* models, int nmodels,
+                        const vxl_instance* instances, int n, int32_t* d_aabb, void* stream);
+
+/* One moved entity (ShadowVoxSystem::OnUpdate): previous and current world
+ * matrices (column-major), pivot, model index. */
+typedef struct vxl_entity {
+    float prev_world[16];
+    float world[16];
+    float pivot[3];
+    int32_t model;
+} vxl_entity;
+
+/* ShadowVoxSystem::OnUpdate (ShadowVoxSystem.cpp:116-191): entities in order,
+ * each clears its previous pose then sets its current one. regions (optional,
+ * host int32[n][6]) receives the dirty byte region x,y,z,w,h,d per entity
+ * (:180-190), or -1s when the reference would push none. Synchronous. */
+vxl_status vxl_shadowvox_update(vxl_ctx* ctx, vxl_grid* grid, const vxl_model* models, int nmodels,
+                                const vxl_entity* entities, int n, int32_t* h_regions, void* stream);
+/* ShadowVoxSystem::OnVoxDestroyed (ShadowVoxSystem.cpp:7-53): clears the
+ * model at `world` (no -Pivot, as the reference). region as above. */
+vxl_status vxl_vox_destroyed(vxl_ctx* ctx, vxl_grid* grid, const vxl_model* model, const float world[16],
+                             int32_t* h_region, void* stream);
+
+/* .v asset reader (VoxAsset::Serialize, VoxAsset.h:42-50): u32 sx,sy,sz then
+ * sx*sy*sz bytes. Query with data == NULL to get the sizes, then read into a
+ * host buffer of sx*sy*sz bytes. */
+vxl_status vxl_read_v(const char* path, int32_t* sx, int32_t* sy, int32_t* sz, uint8_t* h_data, size_t capacity);
+
+/* ---------------------------------------------------- synthetic scenes
+ * Seeded generators for benchmarks and tests (not part of the reference). */
+/* OR into the grid: voxels where the 3-octave value noise at the voxel
+ * centre exceeds thresh, plus the slab y < ground_y */
+vxl_status vxl_scene_noise(vxl_ctx* ctx, vxl_grid* grid, uint32_t seed, float thresh, float freq, int ground_y,
+                           void* stream);
+/* OR into the grid: nboxes seeded axis-aligned boxes with edges in [smin, smax] */
+vxl_status vxl_scene_boxes(vxl_ctx* ctx, vxl_grid* grid, uint32_t seed, int nboxes, int smin, int smax, void* stream);
+/* primary-visibility G-buffer from a pinhole camera (entry-face DDA):
+ * device pos/nrm float[W*H][3], rough float[W*H] */
+vxl_status vxl_scene_gbuffer(vxl_ctx* ctx, const vxl_grid* grid, const float cam[3], const float target[3],
+                             float tan_half_fov, int W, int H, uint32_t seed, float* d_pos, float* d_nrm,
+                             float* d_rough, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VXL_H */

@@ -1,0 +1,882 @@
+// vxl_oracle.cpp — CPU restatement of VoxelEngine's voxel-lighting path.
+//
+// TEST INFRASTRUCTURE ONLY: the parity checker and timed CPU baseline for the
+// CUDA path in voxelengine_gb300/. Nothing in the product links or calls this.
+//
+// Every function cites the reference lines it restates (paths relative to the
+// VoxelEngine source tree). Compiled with -ffp-contract=off so each GLSL/glm
+// operation is one IEEE fp32 rounding, like the CUDA path (built -fmad=false).
+//
+// GLSL built-ins used by the shaders are restated with GLSL semantics:
+//   sign(x)   = x>0 ? 1 : x<0 ? -1 : 0           (+0.0 for +-0 and NaN)
+//   step(e,x) = x<e ? 0 : 1                       (NaN compares give 1)
+//   mod(x,y)  = x - y*floor(x/y)
+//   mix(x,y,a)= x*(1-a) + y*a
+//   int(x)    = truncation toward zero;  ivec / int = truncation toward zero
+//   normalize(v) = v * (1 / sqrt(dot(v,v))), dot = (x*x + y*y) + z*z  (glm's form)
+//   out-of-range texelFetch returns 0 (robust image access)
+// sin/cos are this project's own (Cody-Waite reduction by pi/2 split in three,
+// Taylor polynomials through x^9 / x^10, Horner, no FMA), identical in the CUDA
+// path; they are not the shaders' driver sin/cos.
+#include "vxl_oracle.h"
+
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+namespace {
+
+struct V3 {
+    float x, y, z;
+};
+inline V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+inline V3 add(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline V3 sub(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline V3 mul(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
+inline V3 mulv(V3 a, V3 b) { return v3(a.x * b.x, a.y * b.y, a.z * b.z); }
+inline float dot(V3 a, V3 b) {
+    float t = a.x * b.x + a.y * b.y;
+    return t + a.z * b.z;
+}
+inline V3 cross(V3 a, V3 b) {
+    return v3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+}
+inline float glsl_sign(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
+inline float glsl_step(float e, float x) { return x < e ? 0.0f : 1.0f; }
+inline float glsl_mod(float x, float y) { return x - y * std::floor(x / y); }
+// glm::normalize: v * inversesqrt(dot(v, v)), inversesqrt(x) = 1 / sqrt(x)
+inline V3 normalize(V3 v) {
+    float r = 1.0f / std::sqrt(dot(v, v));
+    return mul(v, r);
+}
+inline V3 mix(V3 a, V3 b, float t) {
+    float u = 1.0f - t;
+    return add(mul(a, u), mul(b, t));
+}
+inline float smoothstep(float e0, float e1, float x) {
+    float t = (x - e0) / (e1 - e0);
+    t = t < 0.0f ? 0.0f : (t > 1.0f ? 1.0f : t);
+    return t * t * (3.0f - 2.0f * t);
+}
+inline V3 load3(const float* p) { return v3(p[0], p[1], p[2]); }
+
+// Inputs outside the shader's defined domain (non-finite, or coordinates that
+// do not fit an int) give a miss with zero fetches, here and in the CUDA path.
+inline bool ray_domain_ok(V3 o, V3 d) {
+    const float lim = 1073741824.0f;  // 2^30
+    return std::isfinite(o.x) && std::isfinite(o.y) && std::isfinite(o.z) && std::isfinite(d.x) &&
+           std::isfinite(d.y) && std::isfinite(d.z) && std::fabs(o.x) < lim && std::fabs(o.y) < lim &&
+           std::fabs(o.z) < lim;
+}
+
+struct Grid {
+    const uint8_t* g;
+    int sx, sy, sz;
+    // texelFetch(SHADOW_VOX_TEXTURE, pos, 0).r with robust out-of-range = 0
+    inline uint32_t texel(int x, int y, int z) const {
+        if (x < 0 || y < 0 || z < 0 || x >= sx || y >= sy || z >= sz) return 0u;
+        return g[(size_t)x + (size_t)y * sx + (size_t)z * sx * sy];
+    }
+    // getVolumeAt, Sources/Shaders/lib/Light.frag:14-27
+    inline bool volume_at(int x, int y, int z, int mip) const {
+        int bit = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
+        int mask = 1 << bit;
+        x /= 2;
+        y /= 2;
+        z /= 2;
+        uint32_t voxel = texel(x, y, z);  // realMip = mip/2 = 0: ShadowVox has one mip
+        if (mip % 2 == 1) return voxel != 0u;
+        return (voxel & (uint32_t)mask) != 0u;
+    }
+};
+
+template <typename F>
+void parallel_for(int n, int threads, F&& f) {
+    if (threads <= 1 || n < 256) {
+        for (int i = 0; i < n; i++) f(i);
+        return;
+    }
+    std::atomic<int> next{0};
+    const int chunk = 64;
+    auto worker = [&]() {
+        for (;;) {
+            int s = next.fetch_add(chunk);
+            if (s >= n) break;
+            int e = s + chunk < n ? s + chunk : n;
+            for (int i = s; i < e; i++) f(i);
+        }
+    };
+    std::vector<std::thread> ts;
+    for (int t = 0; t < threads; t++) ts.emplace_back(worker);
+    for (auto& t : ts) t.join();
+}
+
+// ---------------------------------------------------------------------------
+// raycastShadowVolume, Sources/Shaders/lib/Light.frag:29-81 (mip 0 only: the
+// outer `++i < 4` loop re-runs an identical pass, see vo_dda_literal).
+int dda(const Grid& G, V3 o, V3 d, float maxt, vo_rec* r) {
+    vo_rec rec{0, 0, 0, 0.0f, 0, 0};
+    if (!ray_domain_ok(o, d)) {
+        rec.flags = VO_F_EXIT_BOUNDS;
+        if (r) *r = rec;
+        return 0;
+    }
+    V3 ss = v3(glsl_sign(d.x), glsl_sign(d.y), glsl_sign(d.z));
+    V3 td = v3(1.0f / (d.x * ss.x), 1.0f / (d.y * ss.y), 1.0f / (d.z * ss.z));
+    int cx = (int)std::floor(o.x), cy = (int)std::floor(o.y), cz = (int)std::floor(o.z);
+    V3 nb = v3((float)cx + (ss.x * 0.5f + 0.5f), (float)cy + (ss.y * 0.5f + 0.5f),
+               (float)cz + (ss.z * 0.5f + 0.5f));
+    V3 tm = v3((nb.x - o.x) / d.x, (nb.y - o.y) / d.y, (nb.z - o.z) / d.z);
+    // clamp(current_voxel, ivec3(0), ivec3(u_VolumeDimension/mipSize)*2+1)
+    const int ux = G.sx * 2 + 1, uy = G.sy * 2 + 1, uz = G.sz * 2 + 1;
+    int n = 0;
+    float totalt = 0.0f;
+    do {
+        float selx = glsl_step(tm.x, tm.z) * glsl_step(tm.x, tm.y);
+        float sely = glsl_step(tm.y, tm.x) * glsl_step(tm.y, tm.z);
+        float selz = glsl_step(tm.z, tm.y) * glsl_step(tm.z, tm.x);
+        rec.vx = cx;
+        rec.vy = cy;
+        rec.vz = cz;
+        if (cx < 0 || cy < 0 || cz < 0 || cx > ux || cy > uy || cz > uz) {
+            rec.flags |= VO_F_EXIT_BOUNDS;
+            rec.t = totalt;
+            if (r) *r = rec;
+            return 0;
+        }
+        rec.steps++;
+        bool voxel = G.volume_at(cx, cy, cz, 0);
+        float best_t = tm.x * selx + tm.y * sely;
+        best_t = best_t + tm.z * selz;
+        if (voxel) {
+            rec.t = best_t;
+            rec.flags = VO_F_HIT | (selx != 0.0f ? VO_F_SELX : 0) | (sely != 0.0f ? VO_F_SELY : 0) |
+                        (selz != 0.0f ? VO_F_SELZ : 0);
+            if (r) *r = rec;
+            return 1;
+        }
+        cx += (int)(selx * ss.x);
+        cy += (int)(sely * ss.y);
+        cz += (int)(selz * ss.z);
+        tm.x += td.x * selx;
+        tm.y += td.y * sely;
+        tm.z += td.z * selz;
+        totalt = best_t;
+    } while (++n < 256 && totalt < maxt);
+    rec.flags |= (n >= 256) ? VO_F_EXIT_STEPS : VO_F_EXIT_MAXT;
+    rec.t = totalt;
+    if (r) *r = rec;
+    return 0;
+}
+
+// Shared body of raycastShadowVolumeSparse / SuperSparse,
+// Sources/Shaders/lib/Light.frag:131-173 and :175-217.
+float march(const Grid& G, V3 origin, V3 dir, float dist, float step0, vo_rec* r) {
+    vo_rec rec{0, 0, 0, dist, 0, 0};
+    if (!ray_domain_ok(origin, dir)) {
+        if (r) *r = rec;
+        return dist;
+    }
+    float stepFactor = step0;
+    V3 stepDir = mul(dir, stepFactor);
+    V3 pos = origin;
+    float d = stepFactor;
+    while (d < 16.0f) {
+        // texelFetch(SHADOW_VOX_TEXTURE, ivec3(pos/2), 0).r
+        int bx = (int)(pos.x / 2.0f), by = (int)(pos.y / 2.0f), bz = (int)(pos.z / 2.0f);
+        uint32_t vol = G.texel(bx, by, bz);
+        uint32_t bit = 0u;
+        int qx = glsl_mod(pos.x, 0.5f) > 0.25f, qy = glsl_mod(pos.y, 0.5f) > 0.25f,
+            qz = glsl_mod(pos.z, 0.5f) > 0.25f;
+        bit += qx ? 1u : 0u;
+        bit += qy ? 2u : 0u;
+        bit += qz ? 4u : 0u;
+        uint32_t mask = 1u << bit;
+        rec.steps++;
+        rec.vx = bx * 2 + qx;
+        rec.vy = by * 2 + qy;
+        rec.vz = bz * 2 + qz;
+        if ((mask & vol) != 0u) {
+            rec.t = d;
+            rec.flags = VO_F_HIT;
+            if (r) *r = rec;
+            return d;
+        }
+        pos = add(pos, stepDir);
+        d += stepFactor;
+    }
+    stepFactor *= 2.0f;
+    stepDir = mul(stepDir, 2.0f);
+    float lod1MaxT = dist < 164.0f ? dist : 164.0f;
+    while (d < lod1MaxT) {
+        // getVolumeAt(ivec3(pos), 1)
+        int ix = (int)pos.x, iy = (int)pos.y, iz = (int)pos.z;
+        rec.steps++;
+        rec.vx = (ix / 2) * 2;
+        rec.vy = (iy / 2) * 2;
+        rec.vz = (iz / 2) * 2;
+        if (G.volume_at(ix, iy, iz, 1)) {
+            rec.t = d;
+            rec.flags = VO_F_HIT | VO_F_COARSE;
+            if (r) *r = rec;
+            return d;
+        }
+        pos = add(pos, stepDir);
+        d += stepFactor;
+    }
+    if (r) *r = rec;
+    return dist;
+}
+
+// ---------------------------------------------------------------------------
+// sin/cos: own implementation (see file header)
+const float kTwoOverPi = 0.6366197466850281f;
+const float kP1 = 1.5703125f;
+const float kP2 = 0.0004838705062866211f;
+const float kP3 = -4.371138828673793e-08f;
+
+void sincos_own(float x, float* s, float* c) {
+    float kf = std::rint(x * kTwoOverPi);
+    int k = (int)kf;
+    float r = x - kf * kP1;
+    r = r - kf * kP2;
+    r = r - kf * kP3;
+    float r2 = r * r;
+    float ps = -1.9841270113829523e-04f + r2 * 2.7557318844628753e-06f;
+    ps = 8.333333767950535e-03f + r2 * ps;
+    ps = -1.666666716337204e-01f + r2 * ps;
+    float sn = r + (r * r2) * ps;
+    float pc = 2.4801587642286904e-05f + r2 * -2.755731998149713e-07f;
+    pc = -1.3888889225199819e-03f + r2 * pc;
+    pc = 4.16666679084301e-02f + r2 * pc;
+    pc = -0.5f + r2 * pc;
+    float cs = 1.0f + r2 * pc;
+    switch (k & 3) {
+        case 0: *s = sn; *c = cs; break;
+        case 1: *s = cs; *c = -sn; break;
+        case 2: *s = -sn; *c = -cs; break;
+        default: *s = -cs; *c = sn; break;
+    }
+}
+
+// PCG hash (Jarzynski & Olano, "Hash Functions for GPU Rendering", JCGT 2020)
+inline uint32_t pcg(uint32_t v) {
+    uint32_t state = v * 747796405u + 2891336453u;
+    uint32_t word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+    return (word >> 22u) ^ word;
+}
+inline float u01(uint32_t h) { return (float)(h >> 8) * (1.0f / 16777216.0f); }
+inline float rand01(uint32_t seed, uint32_t pixel, uint32_t sample) {
+    return u01(pcg(pcg(pcg(seed) + pixel) + sample));
+}
+
+// cosineSampleHemisphere, Sources/Shaders/LightAmbient.frag:81-87
+inline V3 cosine_sample(float u1, float u2) {
+    float r = std::sqrt(u1);
+    float theta = 6.283f * u2;
+    float s, c;
+    sincos_own(theta, &s, &c);
+    float x = r * c;
+    float y = r * s;
+    float z1 = 1.0f - u1;
+    return v3(x, y, std::sqrt(z1 > 0.0f ? z1 : 0.0f));
+}
+
+// tangent frame of calculateAmbientIrradiance, Sources/Shaders/LightAmbient.frag:112-113
+inline void tangent_frame(V3 n, V3* t, V3* b) {
+    *t = std::fabs(n.z) > 0.5f ? v3(0.0f, -n.z, n.y) : v3(-n.y, n.x, 0.0f);
+    *b = cross(n, *t);
+}
+inline V3 frame_dir(V3 t, V3 b, V3 n, V3 l) { return add(add(mul(t, l.x), mul(b, l.y)), mul(n, l.z)); }
+
+// ---------------------------------------------------------------------------
+// DDA-mode per-pixel occlusion (this library's ray generator over the
+// reference DDA). Sample ids: spec j -> (2j, 2j+1), AO k -> (64+2k, 65+2k).
+void occlusion_pixel(const Grid& G, const float* pos, const float* nrm, const float* rough, int i,
+                     const vo_params& p, float* shadow, float* ao, float* ao_vis, float* spec,
+                     float* spec_t, vo_rec* recs) {
+    const int R = p.n_shadow + p.n_ao + p.n_spec;
+    V3 P = load3(pos + 3 * (size_t)i), N = load3(nrm + 3 * (size_t)i);
+    if (N.x == 0.0f && N.y == 0.0f && N.z == 0.0f) {  // sky pixel: nothing traced
+        if (shadow) shadow[i] = 1.0f;
+        if (ao) ao[i] = 1.0f;
+        if (ao_vis) ao_vis[i] = 1.0f;
+        if (spec) spec[i] = 1.0f;
+        if (spec_t) spec_t[i] = p.spec_len;
+        if (recs)
+            for (int k = 0; k < R; k++) recs[(size_t)i * R + k] = vo_rec{0, 0, 0, 0.0f, 0, 0};
+        return;
+    }
+    V3 O = add(P, mul(N, p.bias));
+    int slot = 0;
+    float sh = 1.0f;
+    if (p.n_shadow > 0) {
+        vo_rec rr;
+        int h = dda(G, O, load3(p.light_dir), p.shadow_len, &rr);
+        sh = h ? 0.0f : 1.0f;
+        if (recs) recs[(size_t)i * R + slot] = rr;
+        slot++;
+    }
+    V3 T, B;
+    tangent_frame(N, &T, &B);
+    float acc = 0.0f, vis = 0.0f;
+    for (int k = 0; k < p.n_ao; k++) {
+        float u1 = rand01(p.seed, (uint32_t)i, 64u + 2u * k);
+        float u2 = rand01(p.seed, (uint32_t)i, 65u + 2u * k);
+        V3 l = cosine_sample(u1, u2);
+        V3 d = frame_dir(T, B, N, l);
+        vo_rec rr;
+        int h = dda(G, O, d, p.ao_len, &rr);
+        float tt = h ? (rr.t < p.ao_len ? rr.t : p.ao_len) : p.ao_len;
+        float q = tt / p.ao_len;
+        acc += q * q;
+        vis += h ? 0.0f : 1.0f;
+        if (recs) recs[(size_t)i * R + slot] = rr;
+        slot++;
+    }
+    float sp = 0.0f, st = 0.0f;
+    if (p.n_spec > 0) {
+        float ro = rough ? rough[i] : p.default_rough;
+        float a = ro * ro;
+        float a2 = a * a;
+        V3 V = normalize(sub(load3(p.cam_pos), P));
+        for (int j = 0; j < p.n_spec; j++) {
+            float u1 = rand01(p.seed, (uint32_t)i, 2u * j);
+            float u2 = rand01(p.seed, (uint32_t)i, 2u * j + 1u);
+            float ct = std::sqrt((1.0f - u1) / (1.0f + (a2 - 1.0f) * u1));
+            float st2 = 1.0f - ct * ct;
+            float sn = std::sqrt(st2 > 0.0f ? st2 : 0.0f);
+            float s, c;
+            sincos_own(6.2831855f * u2, &s, &c);
+            V3 H = frame_dir(T, B, N, v3(sn * c, sn * s, ct));
+            float vh = dot(V, H);
+            V3 Rf = sub(mul(H, 2.0f * vh), V);
+            V3 d = normalize(Rf);
+            vo_rec rr;
+            int h = dda(G, O, d, p.spec_len, &rr);
+            sp += h ? 0.0f : 1.0f;
+            st += h ? rr.t : p.spec_len;
+            if (recs) recs[(size_t)i * R + slot] = rr;
+            slot++;
+        }
+    }
+    if (shadow) shadow[i] = sh;
+    if (ao) ao[i] = p.n_ao > 0 ? acc / (float)p.n_ao : 1.0f;
+    if (ao_vis) ao_vis[i] = p.n_ao > 0 ? vis / (float)p.n_ao : 1.0f;
+    if (spec) spec[i] = p.n_spec > 0 ? sp / (float)p.n_spec : 1.0f;
+    if (spec_t) spec_t[i] = p.n_spec > 0 ? st / (float)p.n_spec : p.spec_len;
+}
+
+// value noise with a PCG lattice, smoothstep-weighted trilinear
+inline float lattice(int ix, int iy, int iz, uint32_t seed) {
+    return u01(pcg((uint32_t)ix + pcg((uint32_t)iy + pcg((uint32_t)iz + seed))));
+}
+float value_noise3(float x, float y, float z, uint32_t seed) {
+    float fx0 = std::floor(x), fy0 = std::floor(y), fz0 = std::floor(z);
+    int ix = (int)fx0, iy = (int)fy0, iz = (int)fz0;
+    float fx = x - fx0, fy = y - fy0, fz = z - fz0;
+    float wx = fx * fx * (3.0f - 2.0f * fx);
+    float wy = fy * fy * (3.0f - 2.0f * fy);
+    float wz = fz * fz * (3.0f - 2.0f * fz);
+    float c000 = lattice(ix, iy, iz, seed), c100 = lattice(ix + 1, iy, iz, seed);
+    float c010 = lattice(ix, iy + 1, iz, seed), c110 = lattice(ix + 1, iy + 1, iz, seed);
+    float c001 = lattice(ix, iy, iz + 1, seed), c101 = lattice(ix + 1, iy, iz + 1, seed);
+    float c011 = lattice(ix, iy + 1, iz + 1, seed), c111 = lattice(ix + 1, iy + 1, iz + 1, seed);
+    float x00 = c000 + (c100 - c000) * wx;
+    float x10 = c010 + (c110 - c010) * wx;
+    float x01 = c001 + (c101 - c001) * wx;
+    float x11 = c011 + (c111 - c011) * wx;
+    float y0 = x00 + (x10 - x00) * wy;
+    float y1 = x01 + (x11 - x01) * wy;
+    return y0 + (y1 - y0) * wz;
+}
+// octave sum convention of Sources/Util/Noise.cpp:108-122 (amplitude x0.5,
+// frequency x2, normalised by the amplitude sum); octave i uses seed + i*0x9E3779B9
+float noise_octaves(float x, float y, float z, uint32_t seed, float freq, int octaves) {
+    float total = 0.0f, frequency = freq, amplitude = 1.0f, maxValue = 0.0f;
+    for (int i = 0; i < octaves; i++) {
+        total += value_noise3(x * frequency, y * frequency, z * frequency, seed + (uint32_t)i * 0x9E3779B9u) *
+                 amplitude;
+        maxValue += amplitude;
+        amplitude *= 0.5f;
+        frequency *= 2.0f;
+    }
+    return total / maxValue;
+}
+
+inline void set_fine(uint8_t* g, int sx, int sy, int x, int y, int z) {
+    int bit = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
+    g[(size_t)(x >> 1) + (size_t)(y >> 1) * sx + (size_t)(z >> 1) * sx * sy] |= (uint8_t)(1u << bit);
+}
+
+// ShadowVoxSystem::SetVolumeAt, Sources/World/Systems/ShadowVoxSystem.cpp:82-94
+inline void set_volume_at(uint8_t* g, int sx, int sy, int sz, int x, int y, int z, int value) {
+    if (x < 0 || y < 0 || z < 0 || x >= sx * 2 || y >= sy * 2 || z >= sz * 2) return;
+    int bit = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
+    int mask = 1 << bit;
+    x /= 2;
+    y /= 2;
+    z /= 2;
+    uint8_t* data = g + ((size_t)x + ((size_t)y * (size_t)sx) + ((size_t)z * (size_t)sx * sy));
+    *data = (uint8_t)((*data & ~mask) | (value << bit));
+}
+
+// inner loops of ShadowVoxSystem::OnUpdate, Sources/World/Systems/ShadowVoxSystem.cpp:137-155
+// (and :159-177; :22-40 for OnVoxDestroyed). M is column-major 4x4.
+void voxelize_model(uint8_t* g, int sx, int sy, int sz, const uint8_t* model, int msx, int msy, int msz,
+                    const float* M, int value, int* aabb) {
+    V3 o = v3(M[12], M[13], M[14]);
+    V3 dx = v3(M[0] * 0.1f, M[1] * 0.1f, M[2] * 0.1f);
+    V3 dy = v3(M[4] * 0.1f, M[5] * 0.1f, M[6] * 0.1f);
+    V3 dz = v3(M[8] * 0.1f, M[9] * 0.1f, M[10] * 0.1f);
+    for (int z = 0; z < msz; z++)
+        for (int y = 0; y < msy; y++)
+            for (int x = 0; x < msx; x++) {
+                // VoxAsset::PixelAt, Sources/Asset/VoxAsset.h:52-56
+                uint8_t v = model[(size_t)x + (size_t)y * msx + (size_t)z * msx * msy];
+                if (v >= 16) {
+                    V3 wp = add(add(add(o, mul(dx, (float)x)), mul(dy, (float)y)), mul(dz, (float)z));
+                    int fx = (int)(wp.x * 10.0f), fy = (int)(wp.y * 10.0f), fz = (int)(wp.z * 10.0f);
+                    if (aabb) {
+                        if (fx < aabb[0]) aabb[0] = fx;
+                        if (fy < aabb[1]) aabb[1] = fy;
+                        if (fz < aabb[2]) aabb[2] = fz;
+                        if (fx > aabb[3]) aabb[3] = fx;
+                        if (fy > aabb[4]) aabb[4] = fy;
+                        if (fz > aabb[5]) aabb[5] = fz;
+                    }
+                    set_volume_at(g, sx, sy, sz, fx, fy, fz, value);
+                }
+            }
+}
+
+// glm::translate(m, v): Result[3] = m[0]*v[0] + m[1]*v[1] + m[2]*v[2] + m[3]
+void translate(const float* m, const float* v, float* out) {
+    std::memcpy(out, m, 16 * sizeof(float));
+    for (int r = 0; r < 4; r++) {
+        float a = m[0 + r] * v[0] + m[4 + r] * v[1];
+        a = a + m[8 + r] * v[2];
+        out[12 + r] = a + m[12 + r];
+    }
+}
+
+// dirty-region tail of OnUpdate, Sources/World/Systems/ShadowVoxSystem.cpp:180-190
+void region_from_aabb(const int* aabb, int sx, int sy, int sz, int* region) {
+    if (aabb[3] != 0 || aabb[4] != 0 || aabb[5] != 0) {
+        int mn[3] = {aabb[0] / 2, aabb[1] / 2, aabb[2] / 2};
+        int mx[3] = {aabb[3] / 2, aabb[4] / 2, aabb[5] / 2};
+        int lim[3] = {sx - 1, sy - 1, sz - 1};
+        for (int a = 0; a < 3; a++) {
+            if (mn[a] < 0) mn[a] = 0;
+            if (mx[a] > lim[a]) mx[a] = lim[a];
+            region[a] = mn[a];
+            region[3 + a] = mx[a] - mn[a] + 1;
+        }
+    } else {
+        for (int a = 0; a < 6; a++) region[a] = -1;
+    }
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+int vo_version(void) { return 1; }
+
+void vo_sincos(float x, float* s, float* c) { sincos_own(x, s, c); }
+uint32_t vo_pcg(uint32_t v) { return pcg(v); }
+float vo_rand01(uint32_t seed, uint32_t pixel, uint32_t sample) { return rand01(seed, pixel, sample); }
+
+int vo_get_volume_at(const uint8_t* g, int sx, int sy, int sz, int x, int y, int z, int mip) {
+    Grid G{g, sx, sy, sz};
+    return G.volume_at(x, y, z, mip) ? 1 : 0;
+}
+
+int vo_dda(const uint8_t* g, int sx, int sy, int sz, const float* o, const float* d, float maxt, vo_rec* r) {
+    Grid G{g, sx, sy, sz};
+    return dda(G, load3(o), load3(d), maxt, r);
+}
+
+// Literal restatement of Light.frag:29-81 including the outer `++i < 4` loop and
+// the shared `totalt`; used only by tests to show it equals the single pass.
+int vo_dda_literal(const uint8_t* g, int sx, int sy, int sz, const float* o_in, const float* d_in, float maxt,
+                   float* hit, float* normal, int* fetches) {
+    Grid G{g, sx, sy, sz};
+    V3 origin = load3(o_in), direction = load3(d_in);
+    int nf = 0;
+    if (!ray_domain_ok(origin, direction)) {
+        if (fetches) *fetches = 0;
+        return 0;
+    }
+    V3 stepSign = v3(glsl_sign(direction.x), glsl_sign(direction.y), glsl_sign(direction.z));
+    V3 t_delta = v3(1.0f / (direction.x * stepSign.x), 1.0f / (direction.y * stepSign.y),
+                    1.0f / (direction.z * stepSign.z));
+    int mip = 0;
+    int i = 0;
+    float totalt = 0.0f;
+    do {
+        float mipSize = (float)(1 << mip);
+        origin = v3(origin.x / mipSize, origin.y / mipSize, origin.z / mipSize);
+        int cx = (int)std::floor(origin.x), cy = (int)std::floor(origin.y), cz = (int)std::floor(origin.z);
+        V3 nb = v3((float)cx + (stepSign.x * 0.5f + 0.5f), (float)cy + (stepSign.y * 0.5f + 0.5f),
+                   (float)cz + (stepSign.z * 0.5f + 0.5f));
+        V3 t_max = v3((nb.x - origin.x) / direction.x, (nb.y - origin.y) / direction.y,
+                      (nb.z - origin.z) / direction.z);
+        int ux = (int)((float)G.sx / mipSize) * 2 + 1, uy = (int)((float)G.sy / mipSize) * 2 + 1,
+            uz = (int)((float)G.sz / mipSize) * 2 + 1;
+        int n = 0;
+        do {
+            V3 sel = v3(glsl_step(t_max.x, t_max.z) * glsl_step(t_max.x, t_max.y),
+                        glsl_step(t_max.y, t_max.x) * glsl_step(t_max.y, t_max.z),
+                        glsl_step(t_max.z, t_max.y) * glsl_step(t_max.z, t_max.x));
+            if (cx < 0 || cy < 0 || cz < 0 || cx > ux || cy > uy || cz > uz) {
+                if (fetches) *fetches = nf;
+                return 0;
+            }
+            nf++;
+            bool voxel = G.volume_at(cx, cy, cz, mip);
+            float best_t = dot(t_max, sel);
+            if (voxel) {
+                if (normal) {
+                    normal[0] = -stepSign.x * sel.x;
+                    normal[1] = -stepSign.y * sel.y;
+                    normal[2] = -stepSign.z * sel.z;
+                }
+                if (hit) {
+                    V3 h = mul(add(origin, mul(direction, best_t)), mipSize);
+                    hit[0] = h.x;
+                    hit[1] = h.y;
+                    hit[2] = h.z;
+                }
+                if (fetches) *fetches = nf;
+                return 1;
+            }
+            cx += (int)(sel.x * stepSign.x);
+            cy += (int)(sel.y * stepSign.y);
+            cz += (int)(sel.z * stepSign.z);
+            t_max = add(t_max, mulv(t_delta, sel));
+            totalt = best_t;
+        } while (++n < 256 && totalt < maxt);
+        origin = mul(origin, mipSize);
+    } while (++i < 4);
+    if (fetches) *fetches = nf;
+    return 0;
+}
+
+float vo_sparse(const uint8_t* g, int sx, int sy, int sz, const float* o, const float* d, float dist, vo_rec* r) {
+    Grid G{g, sx, sy, sz};
+    return march(G, load3(o), load3(d), dist, 0.5f, r);
+}
+float vo_supersparse(const uint8_t* g, int sx, int sy, int sz, const float* o, const float* d, float dist,
+                     vo_rec* r) {
+    Grid G{g, sx, sy, sz};
+    return march(G, load3(o), load3(d), dist, 2.5f, r);
+}
+
+void vo_cosine_sample(float u1, float u2, float* out3) {
+    V3 v = cosine_sample(u1, u2);
+    out3[0] = v.x;
+    out3[1] = v.y;
+    out3[2] = v.z;
+}
+
+void vo_trace_rays(const uint8_t* g, int sx, int sy, int sz, const float* rays, int n, int mode, vo_rec* recs,
+                   int threads) {
+    Grid G{g, sx, sy, sz};
+    parallel_for(n, threads, [&](int i) {
+        const float* q = rays + 7 * (size_t)i;
+        V3 o = load3(q), d = load3(q + 3);
+        if (mode == VO_MODE_DDA)
+            dda(G, o, d, q[6], recs + i);
+        else
+            march(G, o, d, q[6], mode == VO_MODE_SPARSE ? 0.5f : 2.5f, recs + i);
+    });
+}
+
+void vo_occlusion(const uint8_t* g, int sx, int sy, int sz, const float* pos, const float* nrm, const float* rough,
+                  int npix, const vo_params* p, float* shadow, float* ao, float* ao_vis, float* spec, float* spec_t,
+                  vo_rec* recs, int p0, int p1, int threads) {
+    Grid G{g, sx, sy, sz};
+    if (p0 < 0) p0 = 0;
+    if (p1 > npix || p1 < 0) p1 = npix;
+    parallel_for(p1 - p0, threads, [&](int k) {
+        occlusion_pixel(G, pos, nrm, rough, p0 + k, *p, shadow, ao, ao_vis, spec, spec_t, recs);
+    });
+}
+
+// LightAmbient.frag:141-175 from the world-space position already scaled to
+// fine-voxel units (wcp of :150), the world normal, linear depth and the
+// per-pixel blue-noise texel getNoise() (:49-52).
+void vo_light_ambient(const uint8_t* g, int sx, int sy, int sz, const float* wcp_in, const float* nrm,
+                      const float* depth, const float* noise, int npix, float* shadow, float* irradiance,
+                      vo_rec* recs, int threads) {
+    Grid G{g, sx, sy, sz};
+    const V3 SUN_DIR = normalize(v3(0.3f, 0.4f, 0.5f));  // LightAmbient.frag:15
+    parallel_for(npix, threads, [&](int i) {
+        const float* nz = noise + 4 * (size_t)i;
+        V3 normal = load3(nrm + 3 * (size_t)i);
+        V3 wd = SUN_DIR;
+        V3 wcp = load3(wcp_in + 3 * (size_t)i);
+        V3 randomVec = mul(cosine_sample(nz[0], nz[1]), 0.1f);
+        randomVec.z *= glsl_sign(nz[2] - 0.5f);
+        wd = mix(wd, randomVec, 0.5f);
+        wd = normalize(wd);
+        wcp = add(wcp, mul(wd, nz[3] * 1.0f));
+        wcp = add(wcp, mul(randomVec, 2.5f));
+        float bias = smoothstep(0.0f, 0.2f, depth[i]) * 50.0f + 1.5f;
+        V3 o = add(wcp, mul(normal, bias));
+        vo_rec r0, r1;
+        float t = march(G, o, wd, 128.0f, 0.5f, &r0);
+        shadow[i] = (t != 128.0f) ? 0.0f : 1.0f;
+        // calculateAmbientIrradiance, LightAmbient.frag:111-126
+        V3 T, B;
+        tangent_frame(normal, &T, &B);
+        V3 rv = cosine_sample(nz[0], nz[1]);
+        V3 dir = frame_dir(T, B, normal, rv);
+        float dd = march(G, o, dir, 128.0f, 2.5f, &r1) / 128.0f;
+        irradiance[i] = dd * dd * 0.05f;
+        if (recs) {
+            recs[2 * (size_t)i] = r0;
+            recs[2 * (size_t)i + 1] = r1;
+        }
+    });
+}
+
+// LightReflection.frag:92-113: view_r is the world-space reflection vector
+// (InverseView * vec4(R,0)).xyz before normalisation.
+void vo_light_reflection(const uint8_t* g, int sx, int sy, int sz, const float* wcp_in, const float* nrm,
+                         const float* view_r, const float* rough, const float* noise, int npix, float* t_out,
+                         vo_rec* recs, int threads) {
+    Grid G{g, sx, sy, sz};
+    parallel_for(npix, threads, [&](int i) {
+        const float* nz = noise + 4 * (size_t)i;
+        V3 normal = load3(nrm + 3 * (size_t)i);
+        V3 wd = normalize(load3(view_r + 3 * (size_t)i));
+        V3 wcp = load3(wcp_in + 3 * (size_t)i);
+        V3 randomVec = cosine_sample(nz[0], nz[1]);
+        randomVec.z *= glsl_sign(nz[2] - 0.5f);
+        wd = mix(wd, randomVec, rough[i] * 0.1f);
+        wcp = add(wcp, mul(normal, nz[3]));
+        wd = mul(wd, 1.0f + nz[3] * 0.5f);
+        vo_rec r0;
+        t_out[i] = march(G, add(wcp, normal), wd, 256.0f, 0.5f, &r0);
+        if (recs) recs[i] = r0;
+    });
+}
+
+// LightPoint.frag:234-267 (spot = 0) and LightSpot.frag:83-117 (spot = 1);
+// wpos is the world position in world units. Pixels beyond the light's range
+// are discarded by the shader: their output is left untouched.
+void vo_light_point(const uint8_t* g, int sx, int sy, int sz, const float* wpos, const float* nrm, const float* noise,
+                    int npix, const float* light_pos, float range, int spot, float* shadow, vo_rec* recs,
+                    int threads) {
+    Grid G{g, sx, sy, sz};
+    V3 L = load3(light_pos);
+    parallel_for(npix, threads, [&](int i) {
+        const float* nz = noise + 4 * (size_t)i;
+        V3 worldPos = load3(wpos + 3 * (size_t)i);
+        V3 normal = load3(nrm + 3 * (size_t)i);
+        V3 lightDir = sub(L, worldPos);
+        float lightDistance = std::sqrt(dot(lightDir, lightDir));
+        if (lightDistance > range) {
+            if (recs) recs[i] = vo_rec{0, 0, 0, -1.0f, 0, 0};
+            return;
+        }
+        V3 wd;
+        float hitDist;
+        if (spot) {
+            wd = mul(normalize(lightDir), 10.0f);
+            hitDist = lightDistance * 10.0f;
+        } else {
+            wd = lightDir;
+            hitDist = lightDistance * 10.5f;
+        }
+        V3 wcp = mul(worldPos, 10.0f);
+        V3 randomVec = mul(cosine_sample(nz[0], nz[1]), 0.1f);
+        randomVec.z *= glsl_sign(nz[2] - 0.5f);
+        wd = mix(wd, randomVec, 0.5f);
+        wd = normalize(wd);
+        wcp = add(wcp, mul(wd, nz[3] * 1.0f));
+        wcp = add(wcp, mul(randomVec, 2.5f));
+        vo_rec r0;
+        float t = march(G, add(wcp, mul(normal, 0.5f)), wd, hitDist, spot ? 2.5f : 0.5f, &r0);
+        shadow[i] = (t < hitDist) ? 0.0f : 1.0f;
+        if (recs) recs[i] = r0;
+    });
+}
+
+float vo_value_noise3(float x, float y, float z, uint32_t seed) { return value_noise3(x, y, z, seed); }
+float vo_noise_octaves(float x, float y, float z, uint32_t seed, float freq, int octaves) {
+    return noise_octaves(x, y, z, seed, freq, octaves);
+}
+
+// Seeded scene: fine voxel (x,y,z) is set where the 3-octave value noise at the
+// voxel centre exceeds `thresh`, or where y < ground_y.
+void vo_scene_noise(uint8_t* g, int sx, int sy, int sz, uint32_t seed, float thresh, float freq, int ground_y,
+                    int threads) {
+    const int nx = 2 * sx, ny = 2 * sy, nz = 2 * sz;
+    std::memset(g, 0, (size_t)sx * sy * sz);
+    // one task per byte-plane pair of z so that tasks write disjoint bytes
+    parallel_for(sz, threads, [&](int bz) {
+        for (int z = 2 * bz; z < 2 * bz + 2; z++)
+            for (int y = 0; y < ny; y++)
+                for (int x = 0; x < nx; x++) {
+                    bool on = y < ground_y;
+                    if (!on) {
+                        float v = noise_octaves((float)x + 0.5f, (float)y + 0.5f, (float)z + 0.5f, seed, freq, 3);
+                        on = v > thresh;
+                    }
+                    if (on) set_fine(g, sx, sy, x, y, z);
+                }
+    });
+}
+
+void vo_box_params(uint32_t seed, int i, int nx, int ny, int nz, int smin, int smax, int* out6) {
+    uint32_t base = pcg(pcg(seed ^ 0x5bd1e995u) + (uint32_t)i);
+    int n[3] = {nx, ny, nz};
+    for (int a = 0; a < 3; a++) {
+        uint32_t r1 = pcg(base + 2u * a), r2 = pcg(base + 2u * a + 1u);
+        int s = smin + (int)(r1 % (uint32_t)(smax - smin + 1));
+        if (s > n[a]) s = n[a];
+        int p = (int)(r2 % (uint32_t)(n[a] - s + 1));
+        out6[a] = p;
+        out6[3 + a] = s;
+    }
+}
+
+void vo_scene_boxes(uint8_t* g, int sx, int sy, int sz, uint32_t seed, int nboxes, int smin, int smax) {
+    for (int i = 0; i < nboxes; i++) {
+        int b[6];
+        vo_box_params(seed, i, 2 * sx, 2 * sy, 2 * sz, smin, smax, b);
+        for (int z = b[2]; z < b[2] + b[5]; z++)
+            for (int y = b[1]; y < b[1] + b[4]; y++)
+                for (int x = b[0]; x < b[0] + b[3]; x++) set_fine(g, sx, sy, x, y, z);
+    }
+}
+
+// Primary visibility: pinhole camera at `cam` looking at `target` (up = +y),
+// rays clipped to the grid box [0, 2*s) and walked with a plain entry-face DDA.
+// pos = cam + dir * t_entry (fine-voxel units), nrm = entry face normal, sky
+// pixels get pos = nrm = 0. rough = 0.05 + 0.95 * U(seed, pixel, 7777).
+void vo_gbuffer(const uint8_t* g, int sx, int sy, int sz, const float* cam_in, const float* target,
+                float tan_half_fov, int W, int H, uint32_t seed, float* pos, float* nrm, float* rough, int threads) {
+    Grid G{g, sx, sy, sz};
+    const int Nd[3] = {2 * sx, 2 * sy, 2 * sz};
+    V3 cam = load3(cam_in);
+    V3 fwd = normalize(sub(load3(target), cam));
+    V3 right = normalize(cross(fwd, v3(0.0f, 1.0f, 0.0f)));
+    V3 upv = cross(right, fwd);
+    float aspect = (float)W / (float)H;
+    parallel_for(W * H, threads, [&](int i) {
+        int px = i % W, py = i / W;
+        float u = (((float)px + 0.5f) * 2.0f / (float)W - 1.0f) * tan_half_fov * aspect;
+        float v = (1.0f - ((float)py + 0.5f) * 2.0f / (float)H) * tan_half_fov;
+        V3 d = normalize(add(add(fwd, mul(right, u)), mul(upv, v)));
+        float dv[3] = {d.x, d.y, d.z}, cv[3] = {cam.x, cam.y, cam.z};
+        for (int a = 0; a < 3; a++)
+            if (dv[a] == 0.0f) dv[a] = 1e-20f;
+        float inv[3], tn[3], tf[3];
+        for (int a = 0; a < 3; a++) {
+            inv[a] = 1.0f / dv[a];
+            float t0 = (0.0f - cv[a]) * inv[a], t1 = ((float)Nd[a] - cv[a]) * inv[a];
+            tn[a] = t0 < t1 ? t0 : t1;
+            tf[a] = t0 < t1 ? t1 : t0;
+        }
+        int ax = 0;
+        float tenter = tn[0];
+        if (tn[1] > tenter) { tenter = tn[1]; ax = 1; }
+        if (tn[2] > tenter) { tenter = tn[2]; ax = 2; }
+        float texit = tf[0] < tf[1] ? tf[0] : tf[1];
+        texit = texit < tf[2] ? texit : tf[2];
+        float* po = pos + 3 * (size_t)i;
+        float* no = nrm + 3 * (size_t)i;
+        po[0] = po[1] = po[2] = 0.0f;
+        no[0] = no[1] = no[2] = 0.0f;
+        rough[i] = 0.05f + 0.95f * rand01(seed, (uint32_t)i, 7777u);
+        if (tenter > texit || texit <= 0.0f) return;
+        float tent = tenter > 0.0f ? tenter : 0.0f;
+        int c[3], st[3];
+        float tmax[3], tdel[3];
+        for (int a = 0; a < 3; a++) {
+            st[a] = dv[a] > 0.0f ? 1 : -1;
+            if (a == ax && tenter > 0.0f) {
+                c[a] = dv[a] > 0.0f ? 0 : Nd[a] - 1;
+            } else {
+                float pa = cv[a] + dv[a] * tent;
+                int ci = (int)std::floor(pa);
+                c[a] = ci < 0 ? 0 : (ci > Nd[a] - 1 ? Nd[a] - 1 : ci);
+            }
+            tmax[a] = ((float)(c[a] + (st[a] > 0 ? 1 : 0)) - cv[a]) * inv[a];
+            tdel[a] = std::fabs(inv[a]);
+        }
+        int last = tenter > 0.0f ? ax : -1;
+        for (int it = 0; it < Nd[0] + Nd[1] + Nd[2] + 3; it++) {
+            if (G.volume_at(c[0], c[1], c[2], 0)) {
+                if (last < 0) return;  // camera inside an occupied cell: no surface
+                po[0] = cv[0] + dv[0] * tent;
+                po[1] = cv[1] + dv[1] * tent;
+                po[2] = cv[2] + dv[2] * tent;
+                no[last] = (float)(-st[last]);
+                return;
+            }
+            int a = (tmax[0] <= tmax[1] && tmax[0] <= tmax[2]) ? 0 : (tmax[1] <= tmax[2] ? 1 : 2);
+            tent = tmax[a];
+            c[a] += st[a];
+            tmax[a] += tdel[a];
+            last = a;
+            if (c[a] < 0 || c[a] >= Nd[a]) return;
+        }
+    });
+}
+
+void vo_set_volume_at(uint8_t* g, int sx, int sy, int sz, int x, int y, int z, int value) {
+    set_volume_at(g, sx, sy, sz, x, y, z, value);
+}
+void vo_voxelize_model(uint8_t* g, int sx, int sy, int sz, const uint8_t* model, int msx, int msy, int msz,
+                       const float* M, int value, int* aabb) {
+    voxelize_model(g, sx, sy, sz, model, msx, msy, msz, M, value, aabb);
+}
+void vo_translate(const float* m, const float* v, float* out) { translate(m, v, out); }
+
+// ShadowVoxSystem::OnUpdate, Sources/World/Systems/ShadowVoxSystem.cpp:116-191:
+// entities in order; each clears its previous pose and sets its current pose
+// (both with translate(-Pivot)); regions[6e..] = dirty byte region (x,y,z,w,h,d)
+// or all -1 when the entity's aabbmax stayed at its start value.
+void vo_shadowvox_update(uint8_t* g, int sx, int sy, int sz, int n, const uint8_t* const* models, const int* mdims,
+                         const float* prev, const float* cur, const float* pivot, int* regions) {
+    for (int e = 0; e < n; e++) {
+        int aabb[6] = {sx - 1, sy - 1, sz - 1, 0, 0, 0};
+        float np[3] = {-pivot[3 * e], -pivot[3 * e + 1], -pivot[3 * e + 2]};
+        float M[16];
+        translate(prev + 16 * (size_t)e, np, M);
+        voxelize_model(g, sx, sy, sz, models[e], mdims[3 * e], mdims[3 * e + 1], mdims[3 * e + 2], M, 0, aabb);
+        translate(cur + 16 * (size_t)e, np, M);
+        voxelize_model(g, sx, sy, sz, models[e], mdims[3 * e], mdims[3 * e + 1], mdims[3 * e + 2], M, 1, aabb);
+        if (regions) region_from_aabb(aabb, sx, sy, sz, regions + 6 * (size_t)e);
+    }
+}
+
+// ShadowVoxSystem::OnVoxDestroyed, Sources/World/Systems/ShadowVoxSystem.cpp:7-53
+// (uses WorldMatrix without the -Pivot translation, as the reference does).
+void vo_vox_destroyed(uint8_t* g, int sx, int sy, int sz, const uint8_t* model, int msx, int msy, int msz,
+                      const float* world, int* region) {
+    int aabb[6] = {sx - 1, sy - 1, sz - 1, 0, 0, 0};
+    voxelize_model(g, sx, sy, sz, model, msx, msy, msz, world, 0, aabb);
+    if (region) region_from_aabb(aabb, sx, sy, sz, region);
+}
+
+// FNV-1a 64-bit over the bytes of s: the std::hash<std::string> of the MSVC
+// toolchain the reference's .pf files were written with (Sources/Asset/Assets.h:207-210).
+uint64_t vo_fnv1a64(const char* s) {
+    uint64_t h = 14695981039346656037ull;
+    for (const unsigned char* p = (const unsigned char*)s; *p; ++p) {
+        h ^= (uint64_t)*p;
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+
+}  // extern "C"

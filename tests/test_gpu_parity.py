@@ -1,0 +1,168 @@
+"""CUDA path vs the oracle, through libvxl's C ABI: ray records (hit cell,
+t bits, fetch count, exit reason) must be identical, and so must the grids
+and the occlusion buffers (bit-exact: both sides are IEEE fp32 without
+contraction)."""
+import numpy as np
+import pytest
+
+import oracle
+from tests import cases
+from tests.gpu_util import assert_recs_equal, dev, empty, export_r8, grid_from_r8, rec_buffer, recs_np
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def g64():
+    return cases.noise_grid(64, seed=3)
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_trace_rays_bit_exact(vxl, ctx, g64, mode):
+    import torch
+
+    G = grid_from_r8(vxl, ctx, g64)
+    rays = np.concatenate([cases.edge_rays(64), cases.random_rays(64, 50000, seed=21 + mode)])
+    want = oracle.trace_rays(g64, rays, mode=mode)
+    rec = rec_buffer(len(rays))
+    vxl.trace_rays(ctx, G, dev(rays), len(rays), mode, rec)
+    torch.cuda.synchronize()
+    assert_recs_equal(recs_np(rec), want, "mode %d" % mode)
+    assert (want["flags"] & 1).any() and not (want["flags"] & 1).all()
+
+
+def test_grid_roundtrip_and_count(vxl, ctx):
+    import torch
+
+    rng = np.random.default_rng(5)
+    for dims in [(64, 64, 64), (6, 10, 14), (130, 66, 34)]:
+        f = rng.random(dims[::-1]) < 0.3
+        r8 = oracle.fine_to_r8(f)
+        G = grid_from_r8(vxl, ctx, r8)
+        assert np.array_equal(export_r8(G), r8)
+        assert G.count() == int(f.sum())
+        pal = np.where(f, rng.integers(16, 256, f.shape), rng.integers(0, 16, f.shape)).astype(np.uint8)
+        G2 = vxl.Grid(ctx, *dims)
+        G2.import_palette(dev(pal), 16)
+        assert np.array_equal(export_r8(G2), r8)
+        G.clear()
+        assert G.count() == 0
+
+
+def test_scene_generators_match_oracle(vxl, ctx):
+    import torch
+
+    for n, seed in [(64, 1), (256, 2)]:
+        G = vxl.Grid(ctx, n, n, n)
+        G.scene_noise(seed, 0.55, 1.0 / 32.0, 8)
+        G.scene_boxes(seed, 50, 4, 48)
+        want = oracle.scene_noise(n, n, n, seed=seed)
+        oracle.scene_boxes(want, seed, 50, 4, 48)
+        assert np.array_equal(export_r8(G), want)
+
+
+def _c1_scene(vxl, ctx, n=256, W=640, H=360, seed=7):
+    import torch
+
+    G = vxl.Grid(ctx, n, n, n)
+    G.scene_noise(seed, 0.55, 1.0 / 32.0, 8)
+    cam = np.array([-0.35 * n, 0.9 * n, -0.45 * n], np.float32)
+    tgt = np.array([n / 2, n / 2, n / 2], np.float32)
+    pos, nrm, rough = empty(W * H * 3, torch.float32), empty(W * H * 3, torch.float32), empty(W * H, torch.float32)
+    vxl.scene_gbuffer(ctx, G, cam, tgt, W, H, seed, pos, nrm, rough)
+    return G, cam, tgt, pos, nrm, rough
+
+
+def test_gbuffer_matches_oracle(vxl, ctx):
+    import torch
+
+    n, W, H = 128, 320, 180
+    G, cam, tgt, pos, nrm, rough = _c1_scene(vxl, ctx, n, W, H)
+    g = export_r8(G)
+    p2, n2, r2 = oracle.gbuffer(g, cam, tgt, W, H, 7)
+    torch.cuda.synchronize()
+    assert np.array_equal(pos.cpu().numpy().reshape(-1, 3).view(np.int32), p2.view(np.int32))
+    assert np.array_equal(nrm.cpu().numpy().reshape(-1, 3), n2)
+    assert np.array_equal(rough.cpu().numpy(), r2)
+    assert (np.abs(n2).sum(1) > 0).mean() > 0.5
+
+
+@pytest.mark.parametrize("n_spec", [0, 1])
+def test_occlusion_c1_bit_exact(vxl, ctx, n_spec):
+    """C1: 256^3 noise grid, 640x360 G-buffer, 1 shadow + 4 AO (L=16) [+ 1 GGX spec]."""
+    import torch
+
+    G, cam, tgt, pos, nrm, rough = _c1_scene(vxl, ctx)
+    npix = 640 * 360
+    P = vxl.make_params(light_dir=(0.3, 0.8, 0.5), cam_pos=cam, n_ao=4, ao_len=16.0, n_spec=n_spec, seed=99)
+    R = 1 + 4 + n_spec
+    outs = {k: empty(npix, torch.float32) for k in ("shadow", "ao", "ao_vis", "spec", "spec_t")}
+    rec = rec_buffer(npix * R)
+    vxl.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, records=rec, **outs)
+    torch.cuda.synchronize()
+    g = export_r8(G)
+    OP = oracle.make_params(light_dir=(0.3, 0.8, 0.5), cam_pos=cam, n_ao=4, ao_len=16.0, n_spec=n_spec, seed=99)
+    want = oracle.occlusion(g, pos.cpu().numpy(), nrm.cpu().numpy(), rough.cpu().numpy(), OP, with_recs=True)
+    assert_recs_equal(recs_np(rec), want["recs"], "records")
+    for k in outs:
+        assert np.array_equal(outs[k].cpu().numpy().view(np.int32), want[k].view(np.int32)), k
+    # without records: same buffers
+    outs2 = {k: empty(npix, torch.float32) for k in outs}
+    vxl.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, **outs2)
+    torch.cuda.synchronize()
+    for k in outs:
+        assert torch.equal(outs[k], outs2[k]), k
+
+
+def test_occlusion_host_entry_matches_device(vxl, ctx):
+    import torch
+
+    G, cam, tgt, pos, nrm, rough = _c1_scene(vxl, ctx, 128, 200, 120)
+    npix = 200 * 120
+    P = vxl.make_params(cam_pos=cam, n_ao=8, ao_len=32.0, n_spec=1, seed=3)
+    outs = {k: empty(npix, torch.float32) for k in ("shadow", "ao", "ao_vis", "spec", "spec_t")}
+    vxl.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, **outs)
+    hp, hn, hr = pos.cpu().pin_memory(), nrm.cpu().pin_memory(), rough.cpu().pin_memory()
+    hout = {k: torch.zeros(npix, dtype=torch.float32).pin_memory() for k in outs}
+    vxl.trace_occlusion_host(ctx, G, hp, hn, hr, npix, P, h_shadow=hout["shadow"], h_ao=hout["ao"],
+                             h_ao_vis=hout["ao_vis"], h_spec=hout["spec"], h_spec_t=hout["spec_t"])
+    torch.cuda.synchronize()
+    for k in outs:
+        assert torch.equal(outs[k].cpu(), hout[k]), k
+
+
+def test_light_passes_bit_exact(vxl, ctx, g64):
+    import torch
+
+    G = grid_from_r8(vxl, ctx, g64)
+    rng = np.random.default_rng(8)
+    n = 20000
+    axes = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1]], np.float32)
+    wcp = rng.uniform(-4, 68, (n, 3)).astype(np.float32)
+    nrm = axes[rng.integers(0, 6, n)]
+    depth = rng.uniform(0, 0.3, n).astype(np.float32)
+    noise = rng.random((n, 4)).astype(np.float32)
+    rough = rng.uniform(0.05, 1, n).astype(np.float32)
+    vr = rng.normal(size=(n, 3)).astype(np.float32)
+    sh, irr, r_amb = oracle.light_ambient(g64, wcp, nrm, depth, noise)
+    d_sh, d_irr, d_rec = empty(n, torch.float32), empty(n, torch.float32), rec_buffer(2 * n)
+    vxl.light_ambient(ctx, G, dev(wcp), dev(nrm), dev(depth), dev(noise), n, d_sh, d_irr, d_rec)
+    t, r_ref = oracle.light_reflection(g64, wcp, nrm, vr, rough, noise)
+    d_t, d_rec2 = empty(n, torch.float32), rec_buffer(n)
+    vxl.light_reflection(ctx, G, dev(wcp), dev(nrm), dev(vr), dev(rough), dev(noise), n, d_t, d_rec2)
+    torch.cuda.synchronize()
+    assert np.array_equal(d_sh.cpu().numpy(), sh)
+    assert np.array_equal(d_irr.cpu().numpy().view(np.int32), irr.view(np.int32))
+    assert_recs_equal(recs_np(d_rec), r_amb, "ambient")
+    assert np.array_equal(d_t.cpu().numpy().view(np.int32), t.view(np.int32))
+    assert_recs_equal(recs_np(d_rec2), r_ref, "reflection")
+    wpos = rng.uniform(0.2, 6.2, (n, 3)).astype(np.float32)
+    for spot in (False, True):
+        lp = np.array([3.2, 4.1, 2.7], np.float32)
+        want, r_pt = oracle.light_point(g64, wpos, nrm, noise, lp, 2.5, spot=spot)
+        d_s = dev(np.full(n, -7.0, np.float32))
+        d_rec3 = rec_buffer(n)
+        vxl.light_point(ctx, G, dev(wpos), dev(nrm), dev(noise), n, lp, 2.5, spot, d_s, d_rec3)
+        torch.cuda.synchronize()
+        assert np.array_equal(d_s.cpu().numpy(), want), spot
+        assert_recs_equal(recs_np(d_rec3), r_pt, "point/spot")

@@ -1,0 +1,359 @@
+"""voxelengine_gb300 — Python binding of libvxl, the GB300 voxel-lighting path.
+
+libvxl (include/vxl.h) is a C-ABI library of hand-written sm_103a CUDA kernels:
+the ShadowVox voxelizer and the voxel ray traversal behind shadows, ambient
+occlusion and specular occlusion of VoxelEngine (Sources/Shaders/lib/Light.frag,
+Sources/World/Systems/ShadowVoxSystem.cpp). This module loads it with ctypes
+and mirrors its entry points; device buffers are torch CUDA tensors (used only
+as device memory and streams). There is no CPU fallback: every call raises if
+the library cannot be loaded or returns an error.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libvxl.so")
+
+VXL_OK = 0
+MODE_DDA, MODE_SPARSE, MODE_SUPERSPARSE = 0, 1, 2
+OP_CLEAR, OP_SET = 0, 1
+RF_HIT, RF_SELX, RF_SELY, RF_SELZ = 1, 2, 4, 8
+RF_EXIT_BOUNDS, RF_EXIT_STEPS, RF_EXIT_MAXT, RF_COARSE = 16, 32, 64, 128
+REC_DTYPE = np.dtype(
+    [("vx", "<i4"), ("vy", "<i4"), ("vz", "<i4"), ("t", "<f4"), ("steps", "<i4"), ("flags", "<i4")]
+)
+REC_BYTES = 24
+
+# every symbol include/vxl.h declares
+EXPORTED = [
+    "vxl_abi_version", "vxl_last_error_string", "vxl_status_string", "vxl_ctx_create", "vxl_ctx_destroy",
+    "vxl_ctx_launch_count", "vxl_grid_create", "vxl_grid_destroy", "vxl_grid_describe", "vxl_grid_clear",
+    "vxl_grid_build_bricks", "vxl_grid_import_r8", "vxl_grid_export_r8", "vxl_grid_import_palette",
+    "vxl_grid_count", "vxl_trace_rays", "vxl_trace_occlusion", "vxl_trace_occlusion_host", "vxl_light_ambient",
+    "vxl_light_reflection", "vxl_light_point", "vxl_voxelize", "vxl_shadowvox_update", "vxl_vox_destroyed",
+    "vxl_read_v", "vxl_scene_noise", "vxl_scene_boxes", "vxl_scene_gbuffer",
+]
+
+
+class VxlError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__("vxl status %d: %s" % (status, msg))
+        self.status = status
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("tx", C.c_int32), ("ty", C.c_int32),
+                ("tz", C.c_int32), ("words", C.c_void_p), ("words_bytes", C.c_size_t), ("tile_mask", C.c_void_p),
+                ("tile_mask_bytes", C.c_size_t)]
+
+
+class GBuffer(C.Structure):
+    _fields_ = [("pos", C.c_void_p), ("nrm", C.c_void_p), ("rough", C.c_void_p), ("npix", C.c_int64),
+                ("width", C.c_int32), ("height", C.c_int32)]
+
+
+class TraceParams(C.Structure):
+    _fields_ = [("light_dir", C.c_float * 3), ("cam_pos", C.c_float * 3), ("bias", C.c_float),
+                ("shadow_len", C.c_float), ("ao_len", C.c_float), ("spec_len", C.c_float),
+                ("default_rough", C.c_float), ("n_shadow", C.c_int32), ("n_ao", C.c_int32), ("n_spec", C.c_int32),
+                ("seed", C.c_uint32), ("mode", C.c_int32)]
+
+
+class Outputs(C.Structure):
+    _fields_ = [("shadow", C.c_void_p), ("ao", C.c_void_p), ("ao_vis", C.c_void_p), ("spec", C.c_void_p),
+                ("spec_t", C.c_void_p), ("records", C.c_void_p)]
+
+
+class Model(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("sx", C.c_int32), ("sy", C.c_int32), ("sz", C.c_int32)]
+
+
+class Instance(C.Structure):
+    _fields_ = [("matrix", C.c_float * 16), ("model", C.c_int32), ("op", C.c_int32)]
+
+
+class Entity(C.Structure):
+    _fields_ = [("prev_world", C.c_float * 16), ("world", C.c_float * 16), ("pivot", C.c_float * 3),
+                ("model", C.c_int32)]
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def build(force: bool = False) -> str:
+    from . import build as _b
+
+    return _b.build(force=force)
+
+
+def lib():
+    """Load libvxl.so (raises if it is missing: there is no fallback path)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libvxl.so not built: run voxelengine_gb300.build() (no CPU fallback exists)")
+        L = C.CDLL(LIB_PATH)
+        vp, i64, f = C.c_void_p, C.c_int64, C.c_float
+        L.vxl_abi_version.restype = C.c_int
+        L.vxl_last_error_string.restype = C.c_char_p
+        L.vxl_status_string.restype = C.c_char_p
+        L.vxl_status_string.argtypes = [C.c_int]
+        L.vxl_ctx_create.argtypes = [C.c_int, C.POINTER(vp)]
+        L.vxl_ctx_destroy.argtypes = [vp]
+        L.vxl_ctx_launch_count.argtypes = [vp, C.POINTER(C.c_uint64)]
+        L.vxl_grid_create.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(vp)]
+        L.vxl_grid_destroy.argtypes = [vp]
+        L.vxl_grid_describe.argtypes = [vp, C.POINTER(GridDesc)]
+        L.vxl_grid_clear.argtypes = [vp, vp]
+        L.vxl_grid_build_bricks.argtypes = [vp, vp]
+        L.vxl_grid_import_r8.argtypes = [vp, vp, vp]
+        L.vxl_grid_export_r8.argtypes = [vp, vp, vp]
+        L.vxl_grid_import_palette.argtypes = [vp, vp, C.c_int, vp]
+        L.vxl_grid_count.argtypes = [vp, C.POINTER(C.c_uint64), vp]
+        L.vxl_trace_rays.argtypes = [vp, vp, vp, i64, C.c_int, vp, vp]
+        L.vxl_trace_occlusion.argtypes = [vp, vp, C.POINTER(GBuffer), C.POINTER(TraceParams), C.POINTER(Outputs), vp]
+        L.vxl_trace_occlusion_host.argtypes = [vp, vp, vp, vp, vp, i64, C.POINTER(TraceParams), vp, vp, vp, vp, vp, vp]
+        L.vxl_light_ambient.argtypes = [vp, vp, vp, vp, vp, vp, i64, vp, vp, vp, vp]
+        L.vxl_light_reflection.argtypes = [vp, vp, vp, vp, vp, vp, vp, i64, vp, vp, vp]
+        L.vxl_light_point.argtypes = [vp, vp, vp, vp, vp, i64, C.POINTER(f * 3), f, C.c_int, vp, vp, vp]
+        L.vxl_voxelize.argtypes = [vp, vp, C.POINTER(Model), C.c_int, C.POINTER(Instance), C.c_int, vp, vp]
+        L.vxl_shadowvox_update.argtypes = [vp, vp, C.POINTER(Model), C.c_int, C.POINTER(Entity), C.c_int, vp, vp]
+        L.vxl_vox_destroyed.argtypes = [vp, vp, C.POINTER(Model), C.POINTER(f * 16), vp, vp]
+        L.vxl_read_v.argtypes = [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), vp,
+                                 C.c_size_t]
+        L.vxl_scene_noise.argtypes = [vp, vp, C.c_uint32, f, f, C.c_int, vp]
+        L.vxl_scene_boxes.argtypes = [vp, vp, C.c_uint32, C.c_int, C.c_int, C.c_int, vp]
+        L.vxl_scene_gbuffer.argtypes = [vp, vp, C.POINTER(f * 3), C.POINTER(f * 3), f, C.c_int, C.c_int, C.c_uint32,
+                                        vp, vp, vp, vp]
+        for name in EXPORTED:
+            if name not in ("vxl_abi_version", "vxl_last_error_string", "vxl_status_string"):
+                getattr(L, name).restype = C.c_int
+        _lib = L
+        return L
+
+
+def check(status: int) -> None:
+    if status != VXL_OK:
+        msg = lib().vxl_last_error_string().decode(errors="replace")
+        raise VxlError(status, msg)
+
+
+def _ptr(t) -> int | None:
+    """Device (or host) address of a torch tensor / numpy array / int / None."""
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return t
+    if isinstance(t, np.ndarray):
+        return t.ctypes.data
+    return t.data_ptr()
+
+
+def _stream(stream) -> int | None:
+    if stream is None:
+        import torch
+
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+def _f3(v):
+    return (C.c_float * 3)(*[float(x) for x in v])
+
+
+class Context:
+    """vxl_ctx on one CUDA device."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        check(lib().vxl_ctx_create(device, C.byref(self._h)))
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    def launch_count(self) -> int:
+        n = C.c_uint64()
+        check(lib().vxl_ctx_launch_count(self._h, C.byref(n)))
+        return n.value
+
+    def close(self):
+        if self._h:
+            lib().vxl_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Grid:
+    """Bit-packed ShadowVox grid of fine dimensions (nx, ny, nz)."""
+
+    def __init__(self, ctx: Context, nx: int, ny: int, nz: int):
+        self.ctx = ctx
+        self._h = C.c_void_p()
+        check(lib().vxl_grid_create(ctx.handle, nx, ny, nz, C.byref(self._h)))
+        self.nx, self.ny, self.nz = nx, ny, nz
+
+    @property
+    def handle(self):
+        return self._h
+
+    def describe(self) -> GridDesc:
+        d = GridDesc()
+        check(lib().vxl_grid_describe(self._h, C.byref(d)))
+        return d
+
+    def clear(self, stream=None):
+        check(lib().vxl_grid_clear(self._h, _stream(stream)))
+
+    def build_bricks(self, stream=None):
+        check(lib().vxl_grid_build_bricks(self._h, _stream(stream)))
+
+    def import_r8(self, d_bytes, stream=None):
+        check(lib().vxl_grid_import_r8(self._h, _ptr(d_bytes), _stream(stream)))
+
+    def export_r8(self, d_bytes, stream=None):
+        check(lib().vxl_grid_export_r8(self._h, _ptr(d_bytes), _stream(stream)))
+
+    def import_palette(self, d_pal, opaque_min=16, stream=None):
+        check(lib().vxl_grid_import_palette(self._h, _ptr(d_pal), opaque_min, _stream(stream)))
+
+    def count(self, stream=None) -> int:
+        n = C.c_uint64()
+        check(lib().vxl_grid_count(self._h, C.byref(n), _stream(stream)))
+        return n.value
+
+    def scene_noise(self, seed, thresh=0.55, freq=1.0 / 32.0, ground_y=8, stream=None):
+        check(lib().vxl_scene_noise(self.ctx.handle, self._h, seed, thresh, freq, ground_y, _stream(stream)))
+
+    def scene_boxes(self, seed, nboxes, smin=4, smax=48, stream=None):
+        check(lib().vxl_scene_boxes(self.ctx.handle, self._h, seed, nboxes, smin, smax, _stream(stream)))
+
+    def close(self):
+        if self._h:
+            lib().vxl_grid_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def make_params(light_dir=(0.3, 0.8, 0.5), cam_pos=(0, 0, 0), bias=0.5, shadow_len=100.0, ao_len=16.0,
+                spec_len=256.0, default_rough=0.5, n_shadow=1, n_ao=4, n_spec=0, seed=1, mode=MODE_DDA):
+    p = TraceParams()
+    ld = np.asarray(light_dir, np.float64)
+    ld = (ld / np.linalg.norm(ld)).astype(np.float32)
+    p.light_dir[:] = [float(v) for v in ld]
+    p.cam_pos[:] = [float(v) for v in np.asarray(cam_pos, np.float32)]
+    p.bias, p.shadow_len, p.ao_len, p.spec_len, p.default_rough = bias, shadow_len, ao_len, spec_len, default_rough
+    p.n_shadow, p.n_ao, p.n_spec, p.seed, p.mode = n_shadow, n_ao, n_spec, seed, mode
+    return p
+
+
+def trace_rays(ctx: Context, grid: Grid, d_rays, n: int, mode: int, d_records, stream=None):
+    check(lib().vxl_trace_rays(ctx.handle, grid.handle, _ptr(d_rays), n, mode, _ptr(d_records), _stream(stream)))
+
+
+def trace_occlusion(ctx: Context, grid: Grid, pos, nrm, rough, npix: int, params: TraceParams, shadow=None,
+                    ao=None, ao_vis=None, spec=None, spec_t=None, records=None, stream=None):
+    gb = GBuffer(_ptr(pos), _ptr(nrm), _ptr(rough), npix, 0, 0)
+    out = Outputs(_ptr(shadow), _ptr(ao), _ptr(ao_vis), _ptr(spec), _ptr(spec_t), _ptr(records))
+    check(lib().vxl_trace_occlusion(ctx.handle, grid.handle, C.byref(gb), C.byref(params), C.byref(out),
+                                    _stream(stream)))
+
+
+def trace_occlusion_host(ctx: Context, grid: Grid, h_pos, h_nrm, h_rough, npix: int, params: TraceParams,
+                         h_shadow=None, h_ao=None, h_ao_vis=None, h_spec=None, h_spec_t=None, stream=None):
+    check(lib().vxl_trace_occlusion_host(ctx.handle, grid.handle, _ptr(h_pos), _ptr(h_nrm), _ptr(h_rough), npix,
+                                         C.byref(params), _ptr(h_shadow), _ptr(h_ao), _ptr(h_ao_vis), _ptr(h_spec),
+                                         _ptr(h_spec_t), _stream(stream)))
+
+
+def light_ambient(ctx, grid, wcp, nrm, depth, noise, npix, shadow, irradiance, records=None, stream=None):
+    check(lib().vxl_light_ambient(ctx.handle, grid.handle, _ptr(wcp), _ptr(nrm), _ptr(depth), _ptr(noise), npix,
+                                  _ptr(shadow), _ptr(irradiance), _ptr(records), _stream(stream)))
+
+
+def light_reflection(ctx, grid, wcp, nrm, view_r, rough, noise, npix, t_out, records=None, stream=None):
+    check(lib().vxl_light_reflection(ctx.handle, grid.handle, _ptr(wcp), _ptr(nrm), _ptr(view_r), _ptr(rough),
+                                     _ptr(noise), npix, _ptr(t_out), _ptr(records), _stream(stream)))
+
+
+def light_point(ctx, grid, wpos, nrm, noise, npix, light_pos, light_range, spot, shadow, records=None, stream=None):
+    check(lib().vxl_light_point(ctx.handle, grid.handle, _ptr(wpos), _ptr(nrm), _ptr(noise), npix,
+                                C.byref(_f3(light_pos)), float(light_range), 1 if spot else 0, _ptr(shadow),
+                                _ptr(records), _stream(stream)))
+
+
+def scene_gbuffer(ctx, grid, cam, target, W, H, seed, d_pos, d_nrm, d_rough, tan_half_fov=0.57735026, stream=None):
+    check(lib().vxl_scene_gbuffer(ctx.handle, grid.handle, C.byref(_f3(cam)), C.byref(_f3(target)),
+                                  float(tan_half_fov), W, H, seed, _ptr(d_pos), _ptr(d_nrm), _ptr(d_rough),
+                                  _stream(stream)))
+
+
+def _models(models):
+    arr = (Model * max(1, len(models)))()
+    for i, (ptr, sx, sy, sz) in enumerate(models):
+        arr[i] = Model(ptr, sx, sy, sz)
+    return arr
+
+
+def voxelize(ctx, grid, models, instances, d_aabb=None, stream=None):
+    """models: list of (device ptr, sx, sy, sz); instances: list of (matrix16, model, op)."""
+    ms = _models(models)
+    arr = (Instance * max(1, len(instances)))()
+    for i, (m, mi, op) in enumerate(instances):
+        arr[i].matrix[:] = [float(x) for x in np.asarray(m, np.float32).reshape(16)]
+        arr[i].model, arr[i].op = mi, op
+    check(lib().vxl_voxelize(ctx.handle, grid.handle, ms, len(models), arr, len(instances), _ptr(d_aabb),
+                             _stream(stream)))
+
+
+def shadowvox_update(ctx, grid, models, entities, stream=None):
+    """entities: list of (prev16, world16, pivot3, model). Returns int32[n,6] dirty regions."""
+    ms = _models(models)
+    arr = (Entity * max(1, len(entities)))()
+    for i, (pw, w, pv, mi) in enumerate(entities):
+        arr[i].prev_world[:] = [float(x) for x in np.asarray(pw, np.float32).reshape(16)]
+        arr[i].world[:] = [float(x) for x in np.asarray(w, np.float32).reshape(16)]
+        arr[i].pivot[:] = [float(x) for x in np.asarray(pv, np.float32).reshape(3)]
+        arr[i].model = mi
+    regions = np.zeros((len(entities), 6), np.int32)
+    check(lib().vxl_shadowvox_update(ctx.handle, grid.handle, ms, len(models), arr, len(entities), _ptr(regions),
+                                     _stream(stream)))
+    return regions
+
+
+def vox_destroyed(ctx, grid, model, world, stream=None):
+    ms = _models([model])
+    w = (C.c_float * 16)(*[float(x) for x in np.asarray(world, np.float32).reshape(16)])
+    region = np.zeros(6, np.int32)
+    check(lib().vxl_vox_destroyed(ctx.handle, grid.handle, ms, C.byref(w), _ptr(region), _stream(stream)))
+    return region
+
+
+def read_v(path: str) -> np.ndarray:
+    """Read a .v asset (u32 sx, sy, sz then bytes) -> uint8[sz, sy, sx]."""
+    sx, sy, sz = C.c_int32(), C.c_int32(), C.c_int32()
+    check(lib().vxl_read_v(path.encode(), C.byref(sx), C.byref(sy), C.byref(sz), None, 0))
+    out = np.zeros((sz.value, sy.value, sx.value), np.uint8)
+    check(lib().vxl_read_v(path.encode(), C.byref(sx), C.byref(sy), C.byref(sz), _ptr(out), out.nbytes))
+    return out

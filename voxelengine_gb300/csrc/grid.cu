@@ -1,0 +1,376 @@
+// grid.cu — grid layout conversions, tile map, and the seeded scene /
+// G-buffer generators used by tests and benchmarks.
+#include "vxl_device.cuh"
+
+namespace vxl {
+
+static GridView view_of(const vxl_grid* g) {
+    GridView v;
+    v.words = g->words;
+    v.tmask = g->tmask;
+    v.nx = g->nx;
+    v.ny = g->ny;
+    v.nz = g->nz;
+    v.tx = g->tx;
+    v.ty = g->ty;
+    v.tz = g->tz;
+    v.txy = (uint32_t)g->tx * (uint32_t)g->ty;
+    return v;
+}
+
+// fine coordinates of bit b of word w (inverse of word_index / bit_index)
+__device__ __forceinline__ void word_origin(const GridView& g, uint32_t w, int* x0, int* y0, int* z0) {
+    uint32_t tile = w >> 3, sub = w & 7u;
+    uint32_t tz = tile / g.txy, rem = tile - tz * g.txy;
+    uint32_t ty = rem / (uint32_t)g.tx, tx = rem - ty * (uint32_t)g.tx;
+    *x0 = (int)(tx * 8u + (sub & 1u) * 4u);
+    *y0 = (int)(ty * 8u + ((sub >> 1) & 1u) * 4u);
+    *z0 = (int)(tz * 8u + ((sub >> 2) & 1u) * 4u);
+}
+
+// ---------------------------------------------------------------- R8 in/out
+// ShadowVox R8 layout: byte (bx,by,bz) at bx + by*sx + bz*sx*sy holds fine
+// voxels 2b + {0,1}^3, bit (x&1)|(y&1)<<1|(z&1)<<2 (ShadowVoxSystem.cpp:82-94).
+__global__ void k_import_r8(GridView g, uint64_t* words, const uint8_t* __restrict__ bytes, uint32_t nwords) {
+    uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nwords) return;
+    int x0, y0, z0;
+    word_origin(g, w, &x0, &y0, &z0);
+    const int sx = g.nx >> 1, sy = g.ny >> 1, sz = g.nz >> 1;
+    uint64_t out = 0;
+    for (int dz = 0; dz < 2; dz++)
+        for (int dy = 0; dy < 2; dy++)
+            for (int dx = 0; dx < 2; dx++) {
+                int bx = (x0 >> 1) + dx, by = (y0 >> 1) + dy, bz = (z0 >> 1) + dz;
+                if (bx >= sx || by >= sy || bz >= sz) continue;
+                uint32_t v = bytes[(size_t)bx + (size_t)by * sx + (size_t)bz * sx * sy];
+                for (int b = 0; b < 8; b++)
+                    if (v & (1u << b)) {
+                        int lx = 2 * dx + (b & 1), ly = 2 * dy + ((b >> 1) & 1), lz = 2 * dz + ((b >> 2) & 1);
+                        out |= 1ull << (lx | (ly << 2) | (lz << 4));
+                    }
+            }
+    words[w] = out;
+}
+
+__global__ void k_export_r8(GridView g, uint8_t* __restrict__ bytes, uint32_t nbytes) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nbytes) return;
+    const uint32_t sx = g.nx >> 1, sy = g.ny >> 1;
+    uint32_t bz = i / (sx * sy), rem = i - bz * sx * sy;
+    uint32_t by = rem / sx, bx = rem - by * sx;
+    int x = 2 * bx, y = 2 * by, z = 2 * bz;
+    uint64_t w = g.words[word_index(g, x, y, z)];
+    uint32_t sh = bit_index(x, y, z);
+    uint32_t v = 0;
+    for (int b = 0; b < 8; b++) {
+        uint32_t bit = sh + (b & 1) + ((b >> 1) & 1) * 4 + ((b >> 2) & 1) * 16;
+        v |= (uint32_t)((w >> bit) & 1ull) << b;
+    }
+    bytes[i] = (uint8_t)v;
+}
+
+// dense palette volume [nz][ny][nx] -> bits (index >= opaque_min)
+__global__ void k_import_palette(GridView g, uint64_t* words, const uint8_t* __restrict__ pal, int opaque_min,
+                                 uint32_t nwords) {
+    uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nwords) return;
+    int x0, y0, z0;
+    word_origin(g, w, &x0, &y0, &z0);
+    uint64_t out = 0;
+    for (int lz = 0; lz < 4; lz++)
+        for (int ly = 0; ly < 4; ly++)
+            for (int lx = 0; lx < 4; lx++) {
+                int x = x0 + lx, y = y0 + ly, z = z0 + lz;
+                if (x >= g.nx || y >= g.ny || z >= g.nz) continue;
+                if (pal[(size_t)x + (size_t)y * g.nx + (size_t)z * g.nx * g.ny] >= opaque_min)
+                    out |= 1ull << (lx | (ly << 2) | (lz << 4));
+            }
+    words[w] = out;
+}
+
+// one bit per 8^3 tile: any of its 8 words non-zero
+__global__ void k_tile_mask(const uint64_t* __restrict__ words, uint32_t* mask, uint32_t ntiles, uint32_t nmask) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nmask * 32u) return;
+    bool any = false;
+    if (t < ntiles) {
+        const ulonglong2* p = reinterpret_cast<const ulonglong2*>(words + (size_t)t * 8u);
+        ulonglong2 a = p[0], b = p[1], c = p[2], d = p[3];
+        any = (a.x | a.y | b.x | b.y | c.x | c.y | d.x | d.y) != 0ull;
+    }
+    unsigned m = __ballot_sync(0xffffffffu, any);
+    if ((threadIdx.x & 31) == 0) mask[t >> 5] = m;
+}
+
+__global__ void k_count(const uint64_t* __restrict__ words, size_t n, unsigned long long* out) {
+    unsigned long long c = 0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        c += __popcll(words[i]);
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+// ------------------------------------------------------------- scene noise
+// value noise with a PCG lattice, smoothstep-weighted trilinear; same
+// arithmetic as the oracle's value_noise3 / noise_octaves
+__device__ __forceinline__ float lattice(int ix, int iy, int iz, uint32_t seed) {
+    return u01(pcg((uint32_t)ix + pcg((uint32_t)iy + pcg((uint32_t)iz + seed))));
+}
+__device__ float value_noise3(float x, float y, float z, uint32_t seed) {
+    float fx0 = floorf(x), fy0 = floorf(y), fz0 = floorf(z);
+    int ix = (int)fx0, iy = (int)fy0, iz = (int)fz0;
+    float fx = x - fx0, fy = y - fy0, fz = z - fz0;
+    float wx = fx * fx * (3.0f - 2.0f * fx);
+    float wy = fy * fy * (3.0f - 2.0f * fy);
+    float wz = fz * fz * (3.0f - 2.0f * fz);
+    float c000 = lattice(ix, iy, iz, seed), c100 = lattice(ix + 1, iy, iz, seed);
+    float c010 = lattice(ix, iy + 1, iz, seed), c110 = lattice(ix + 1, iy + 1, iz, seed);
+    float c001 = lattice(ix, iy, iz + 1, seed), c101 = lattice(ix + 1, iy, iz + 1, seed);
+    float c011 = lattice(ix, iy + 1, iz + 1, seed), c111 = lattice(ix + 1, iy + 1, iz + 1, seed);
+    float x00 = c000 + (c100 - c000) * wx;
+    float x10 = c010 + (c110 - c010) * wx;
+    float x01 = c001 + (c101 - c001) * wx;
+    float x11 = c011 + (c111 - c011) * wx;
+    float y0 = x00 + (x10 - x00) * wy;
+    float y1 = x01 + (x11 - x01) * wy;
+    return y0 + (y1 - y0) * wz;
+}
+// octave convention of Sources/Util/Noise.cpp:108-122
+__device__ float noise_octaves(float x, float y, float z, uint32_t seed, float freq, int octaves) {
+    float total = 0.0f, frequency = freq, amplitude = 1.0f, maxValue = 0.0f;
+    for (int i = 0; i < octaves; i++) {
+        total += value_noise3(x * frequency, y * frequency, z * frequency, seed + (uint32_t)i * 0x9E3779B9u) *
+                 amplitude;
+        maxValue += amplitude;
+        amplitude *= 0.5f;
+        frequency *= 2.0f;
+    }
+    return total / maxValue;
+}
+
+// one thread per word; ORs into the grid
+__global__ void k_scene_noise(GridView g, uint64_t* words, uint32_t seed, float thresh, float freq, int ground_y,
+                              uint32_t nwords) {
+    uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nwords) return;
+    int x0, y0, z0;
+    word_origin(g, w, &x0, &y0, &z0);
+    if (x0 >= g.nx || y0 >= g.ny || z0 >= g.nz) return;
+    uint64_t out = 0;
+    for (int lz = 0; lz < 4; lz++)
+        for (int ly = 0; ly < 4; ly++)
+            for (int lx = 0; lx < 4; lx++) {
+                int x = x0 + lx, y = y0 + ly, z = z0 + lz;
+                if (x >= g.nx || y >= g.ny || z >= g.nz) continue;
+                bool on = y < ground_y;
+                if (!on) on = noise_octaves((float)x + 0.5f, (float)y + 0.5f, (float)z + 0.5f, seed, freq, 3) > thresh;
+                if (on) out |= 1ull << (lx | (ly << 2) | (lz << 4));
+            }
+    if (out) words[w] |= out;
+}
+
+// box i: per axis size smin + pcg(base+2a) % (smax-smin+1) (clamped to the
+// grid), position pcg(base+2a+1) % (n-size+1); base = pcg(pcg(seed^0x5bd1e995)+i)
+__device__ __forceinline__ void box_params(uint32_t seed, int i, const int* n, int smin, int smax, int* b) {
+    uint32_t base = pcg(pcg(seed ^ 0x5bd1e995u) + (uint32_t)i);
+    for (int a = 0; a < 3; a++) {
+        uint32_t r1 = pcg(base + 2u * a), r2 = pcg(base + 2u * a + 1u);
+        int s = smin + (int)(r1 % (uint32_t)(smax - smin + 1));
+        if (s > n[a]) s = n[a];
+        b[a] = (int)(r2 % (uint32_t)(n[a] - s + 1));
+        b[3 + a] = s;
+    }
+}
+// one block per box, threads over the 4^3 bricks it overlaps
+__global__ void k_scene_boxes(GridView g, uint64_t* words, uint32_t seed, int smin, int smax) {
+    int n[3] = {g.nx, g.ny, g.nz};
+    int b[6];
+    box_params(seed, blockIdx.x, n, smin, smax, b);
+    int wx0 = b[0] >> 2, wy0 = b[1] >> 2, wz0 = b[2] >> 2;
+    int wx1 = (b[0] + b[3] - 1) >> 2, wy1 = (b[1] + b[4] - 1) >> 2, wz1 = (b[2] + b[5] - 1) >> 2;
+    int cx = wx1 - wx0 + 1, cy = wy1 - wy0 + 1, cz = wz1 - wz0 + 1;
+    for (int k = threadIdx.x; k < cx * cy * cz; k += blockDim.x) {
+        int bz = wz0 + k / (cx * cy), rem = k % (cx * cy);
+        int by = wy0 + rem / cx, bx = wx0 + rem % cx;
+        uint64_t m = 0;
+        for (int lz = 0; lz < 4; lz++)
+            for (int ly = 0; ly < 4; ly++)
+                for (int lx = 0; lx < 4; lx++) {
+                    int x = 4 * bx + lx, y = 4 * by + ly, z = 4 * bz + lz;
+                    if (x >= b[0] && x < b[0] + b[3] && y >= b[1] && y < b[1] + b[4] && z >= b[2] && z < b[2] + b[5])
+                        m |= 1ull << (lx | (ly << 2) | (lz << 4));
+                }
+        if (m) atomicOr((unsigned long long*)(words + word_index(g, 4 * bx, 4 * by, 4 * bz)), (unsigned long long)m);
+    }
+}
+
+// -------------------------------------------------------------- G-buffer
+// Pinhole camera at cam looking at target (up +y); rays clipped to the grid
+// box and walked with an entry-face DDA (same arithmetic as the oracle's
+// vo_gbuffer). Sky pixels: pos = nrm = 0.
+__global__ void k_gbuffer(GridView g, f3 cam, f3 fwd, f3 right, f3 upv, float tanh_, float aspect, int W, int H,
+                          uint32_t seed_h, float* pos, float* nrm, float* rough) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W * H) return;
+    int px = i % W, py = i / W;
+    const int Nd[3] = {g.nx, g.ny, g.nz};
+    float u = (((float)px + 0.5f) * 2.0f / (float)W - 1.0f) * tanh_ * aspect;
+    float v = (1.0f - ((float)py + 0.5f) * 2.0f / (float)H) * tanh_;
+    f3 d = normalize(add(add(fwd, mul(right, u)), mul(upv, v)));
+    float dv[3] = {d.x, d.y, d.z}, cv[3] = {cam.x, cam.y, cam.z};
+    for (int a = 0; a < 3; a++)
+        if (dv[a] == 0.0f) dv[a] = 1e-20f;
+    float inv[3], tn[3], tf[3];
+    for (int a = 0; a < 3; a++) {
+        inv[a] = 1.0f / dv[a];
+        float t0 = (0.0f - cv[a]) * inv[a], t1 = ((float)Nd[a] - cv[a]) * inv[a];
+        tn[a] = t0 < t1 ? t0 : t1;
+        tf[a] = t0 < t1 ? t1 : t0;
+    }
+    int ax = 0;
+    float tenter = tn[0];
+    if (tn[1] > tenter) { tenter = tn[1]; ax = 1; }
+    if (tn[2] > tenter) { tenter = tn[2]; ax = 2; }
+    float texit = tf[0] < tf[1] ? tf[0] : tf[1];
+    texit = texit < tf[2] ? texit : tf[2];
+    float* po = pos + 3 * (size_t)i;
+    float* no = nrm + 3 * (size_t)i;
+    float P[3] = {0.0f, 0.0f, 0.0f}, Nn[3] = {0.0f, 0.0f, 0.0f};
+    rough[i] = 0.05f + 0.95f * rand01(seed_h, (uint32_t)i, 7777u);
+    if (!(tenter > texit || texit <= 0.0f)) {
+        float tent = tenter > 0.0f ? tenter : 0.0f;
+        int c[3], st[3];
+        float tmax[3], tdel[3];
+        for (int a = 0; a < 3; a++) {
+            st[a] = dv[a] > 0.0f ? 1 : -1;
+            if (a == ax && tenter > 0.0f) {
+                c[a] = dv[a] > 0.0f ? 0 : Nd[a] - 1;
+            } else {
+                float pa = cv[a] + dv[a] * tent;
+                int ci = (int)floorf(pa);
+                c[a] = ci < 0 ? 0 : (ci > Nd[a] - 1 ? Nd[a] - 1 : ci);
+            }
+            tmax[a] = ((float)(c[a] + (st[a] > 0 ? 1 : 0)) - cv[a]) * inv[a];
+            tdel[a] = fabsf(inv[a]);
+        }
+        int last = tenter > 0.0f ? ax : -1;
+        for (int it = 0; it < Nd[0] + Nd[1] + Nd[2] + 3; it++) {
+            if (fine_at(g, c[0], c[1], c[2])) {
+                if (last >= 0) {
+                    for (int a = 0; a < 3; a++) P[a] = cv[a] + dv[a] * tent;
+                    Nn[last] = (float)(-st[last]);
+                }
+                break;
+            }
+            int a = (tmax[0] <= tmax[1] && tmax[0] <= tmax[2]) ? 0 : (tmax[1] <= tmax[2] ? 1 : 2);
+            tent = tmax[a];
+            c[a] += st[a];
+            tmax[a] += tdel[a];
+            last = a;
+            if (c[a] < 0 || c[a] >= Nd[a]) break;
+        }
+    }
+    po[0] = P[0];
+    po[1] = P[1];
+    po[2] = P[2];
+    no[0] = Nn[0];
+    no[1] = Nn[1];
+    no[2] = Nn[2];
+}
+
+// ---------------------------------------------------------------- launchers
+static inline unsigned blocks_for(size_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
+
+vxl_status launch_grid_import_r8(vxl_grid* g, const uint8_t* bytes, cudaStream_t s) {
+    GridView v = view_of(g);
+    k_import_r8<<<blocks_for(g->nwords, 256), 256, 0, s>>>(v, g->words, bytes, (uint32_t)g->nwords);
+    g->ctx->launches++;
+    VXL_TRY_CUDA(cudaGetLastError());
+    return launch_build_tile_mask(g, s);
+}
+
+vxl_status launch_grid_export_r8(const vxl_grid* g, uint8_t* bytes, cudaStream_t s) {
+    GridView v = view_of(g);
+    uint32_t nb = (uint32_t)((size_t)(g->nx / 2) * (g->ny / 2) * (g->nz / 2));
+    k_export_r8<<<blocks_for(nb, 256), 256, 0, s>>>(v, bytes, nb);
+    g->ctx->launches++;
+    VXL_TRY_CUDA(cudaGetLastError());
+    return VXL_OK;
+}
+
+vxl_status launch_grid_import_palette(vxl_grid* g, const uint8_t* pal, int opaque_min, cudaStream_t s) {
+    GridView v = view_of(g);
+    k_import_palette<<<blocks_for(g->nwords, 128), 128, 0, s>>>(v, g->words, pal, opaque_min, (uint32_t)g->nwords);
+    g->ctx->launches++;
+    VXL_TRY_CUDA(cudaGetLastError());
+    return launch_build_tile_mask(g, s);
+}
+
+vxl_status launch_build_tile_mask(vxl_grid* g, cudaStream_t s) {
+    uint32_t ntiles = (uint32_t)(g->nwords / 8);
+    k_tile_mask<<<blocks_for(g->nmask * 32, 256), 256, 0, s>>>(g->words, g->tmask, ntiles, (uint32_t)g->nmask);
+    g->ctx->launches++;
+    VXL_TRY_CUDA(cudaGetLastError());
+    return VXL_OK;
+}
+
+vxl_status launch_grid_count(const vxl_grid* g, unsigned long long* d_out, cudaStream_t s) {
+    k_count<<<g->ctx->sm_count * 4, 256, 0, s>>>(g->words, g->nwords, d_out);
+    g->ctx->launches++;
+    VXL_TRY_CUDA(cudaGetLastError());
+    return VXL_OK;
+}
+
+vxl_status launch_scene_noise(vxl_grid* g, uint32_t seed, float thresh, float freq, int ground_y, cudaStream_t s) {
+    GridView v = view_of(g);
+    k_scene_noise<<<blocks_for(g->nwords, 128), 128, 0, s>>>(v, g->words, seed, thresh, freq, ground_y,
+                                                             (uint32_t)g->nwords);
+    g->ctx->launches++;
+    VXL_TRY_CUDA(cudaGetLastError());
+    return launch_build_tile_mask(g, s);
+}
+
+vxl_status launch_scene_boxes(vxl_grid* g, uint32_t seed, int nboxes, int smin, int smax, cudaStream_t s) {
+    if (nboxes <= 0) return VXL_OK;
+    GridView v = view_of(g);
+    k_scene_boxes<<<nboxes, 128, 0, s>>>(v, g->words, seed, smin, smax);
+    g->ctx->launches++;
+    VXL_TRY_CUDA(cudaGetLastError());
+    return launch_build_tile_mask(g, s);
+}
+
+// host-side camera basis, same arithmetic as the oracle (compiled without FMA contraction)
+static void h_normalize(const float* v, float* o) {
+    float d = v[0] * v[0] + v[1] * v[1];
+    d = d + v[2] * v[2];
+    float r = 1.0f / sqrtf(d);
+    o[0] = v[0] * r;
+    o[1] = v[1] * r;
+    o[2] = v[2] * r;
+}
+static void h_cross(const float* a, const float* b, float* o) {
+    o[0] = a[1] * b[2] - b[1] * a[2];
+    o[1] = a[2] * b[0] - b[2] * a[0];
+    o[2] = a[0] * b[1] - b[0] * a[1];
+}
+
+vxl_status launch_scene_gbuffer(const vxl_grid* g, const float cam[3], const float target[3], float tan_half_fov,
+                                int W, int H, uint32_t seed, float* pos, float* nrm, float* rough, cudaStream_t s) {
+    float t[3] = {target[0] - cam[0], target[1] - cam[1], target[2] - cam[2]};
+    float fwd[3], right[3], upv[3], up[3] = {0.0f, 1.0f, 0.0f}, tmp[3];
+    h_normalize(t, fwd);
+    h_cross(fwd, up, tmp);
+    h_normalize(tmp, right);
+    h_cross(right, fwd, upv);
+    float aspect = (float)W / (float)H;
+    GridView v = view_of(g);
+    k_gbuffer<<<blocks_for((size_t)W * H, 128), 128, 0, s>>>(
+        v, mk(cam[0], cam[1], cam[2]), mk(fwd[0], fwd[1], fwd[2]), mk(right[0], right[1], right[2]),
+        mk(upv[0], upv[1], upv[2]), tan_half_fov, aspect, W, H, pcg(seed), pos, nrm, rough);
+    g->ctx->launches++;
+    VXL_TRY_CUDA(cudaGetLastError());
+    return VXL_OK;
+}
+
+}  // namespace vxl

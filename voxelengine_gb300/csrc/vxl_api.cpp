@@ -1,0 +1,555 @@
+// vxl_api.cpp — host side of libvxl: the C ABI declared in include/vxl.h.
+// Validates arguments, owns contexts and grids, plans voxelizer runs, and
+// dispatches to the kernel launchers. Compiled without FMA contraction so the
+// host-side matrix arithmetic (glm::translate) matches the reference bit for bit.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "vxl_internal.h"
+
+namespace vxl {
+
+static thread_local std::string g_last_error;
+
+vxl_status fail(vxl_status s, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return s;
+}
+
+vxl_status cuda_fail(cudaError_t e, const char* what) {
+    return fail(e == cudaErrorMemoryAllocation ? VXL_ERR_OOM : VXL_ERR_CUDA, "%s: %s (%s)", what,
+                cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+static vxl_status grow(void** p, size_t* have, size_t need) {
+    if (*have >= need) return VXL_OK;
+    size_t n = *have ? *have : (size_t)1 << 20;
+    while (n < need) n *= 2;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *have = 0;
+    cudaError_t e = cudaMalloc(p, n);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(scratch)");
+    *have = n;
+    return VXL_OK;
+}
+
+vxl_status ctx_scratch(vxl_ctx* ctx, size_t bytes, void** out) {
+    VXL_TRY(grow(&ctx->d_scratch, &ctx->d_scratch_bytes, bytes));
+    *out = ctx->d_scratch;
+    return VXL_OK;
+}
+vxl_status ctx_stage(vxl_ctx* ctx, size_t bytes, void** out) {
+    VXL_TRY(grow(&ctx->d_stage, &ctx->d_stage_bytes, bytes));
+    *out = ctx->d_stage;
+    return VXL_OK;
+}
+
+// glm::translate(m, v): Result[3] = m[0]*v[0] + m[1]*v[1] + m[2]*v[2] + m[3]
+static void translate(const float* m, const float* v, float* out) {
+    std::memcpy(out, m, 16 * sizeof(float));
+    for (int r = 0; r < 4; r++) {
+        float a = m[0 + r] * v[0] + m[4 + r] * v[1];
+        a = a + m[8 + r] * v[2];
+        out[12 + r] = a + m[12 + r];
+    }
+}
+
+static vxl_status set_device(const vxl_ctx* ctx) {
+    VXL_TRY_CUDA(cudaSetDevice(ctx->device));
+    return VXL_OK;
+}
+
+static bool grid_ok(const vxl_grid* g) { return g && g->ctx && g->words; }
+
+// Plan a voxelizer run: upload instances/models/chunk table, launch.
+static vxl_status voxelize_runs(vxl_ctx* ctx, vxl_grid* g, const vxl_model* models, int nmodels,
+                                const std::vector<DevInstance>& inst, int32_t* d_aabb, cudaStream_t s) {
+    const int n = (int)inst.size();
+    if (n == 0) return VXL_OK;
+    std::vector<DevModel> dm((size_t)nmodels);
+    for (int i = 0; i < nmodels; i++) dm[i] = DevModel{models[i].data, models[i].sx, models[i].sy, models[i].sz, 0};
+    // chunk tables per run of equal ops, concatenated
+    std::vector<int2> chunks;
+    std::vector<std::pair<size_t, size_t>> runs;  // [begin, end) into chunks
+    std::vector<int> run_value;
+    for (int i = 0; i < n;) {
+        int j = i;
+        size_t b = chunks.size();
+        while (j < n && inst[j].op == inst[i].op) {
+            const DevModel& m = dm[inst[j].model];
+            long long cnt = (long long)m.sx * m.sy * m.sz;
+            for (long long v = 0; v < cnt; v += kVoxChunk) chunks.push_back(make_int2(j, (int)v));
+            j++;
+        }
+        runs.push_back({b, chunks.size()});
+        run_value.push_back(inst[i].op == VXL_OP_SET ? 1 : 0);
+        i = j;
+    }
+    size_t b_inst = inst.size() * sizeof(DevInstance);
+    size_t b_mod = dm.size() * sizeof(DevModel);
+    size_t b_ch = chunks.size() * sizeof(int2);
+    size_t off_mod = (b_inst + 255) & ~(size_t)255, off_ch = (off_mod + b_mod + 255) & ~(size_t)255;
+    void* scratch;
+    VXL_TRY(ctx_scratch(ctx, off_ch + b_ch + 256, &scratch));
+    char* base = (char*)scratch;
+    VXL_TRY_CUDA(cudaMemcpyAsync(base, inst.data(), b_inst, cudaMemcpyHostToDevice, s));
+    VXL_TRY_CUDA(cudaMemcpyAsync(base + off_mod, dm.data(), b_mod, cudaMemcpyHostToDevice, s));
+    if (b_ch) VXL_TRY_CUDA(cudaMemcpyAsync(base + off_ch, chunks.data(), b_ch, cudaMemcpyHostToDevice, s));
+    const DevInstance* d_inst = (const DevInstance*)base;
+    const DevModel* d_mod = (const DevModel*)(base + off_mod);
+    const int2* d_ch = (const int2*)(base + off_ch);
+    for (size_t r = 0; r < runs.size(); r++) {
+        int nch = (int)(runs[r].second - runs[r].first);
+        VXL_TRY(launch_voxelize_run(g, d_inst, d_mod, d_ch + runs[r].first, nch, run_value[r], d_aabb, s));
+    }
+    // the host vectors must outlive the async copies
+    VXL_TRY_CUDA(cudaStreamSynchronize(s));
+    return launch_build_tile_mask(g, s);
+}
+
+static vxl_status check_models(const vxl_model* models, int nmodels) {
+    if (nmodels < 0 || (nmodels > 0 && !models)) return fail(VXL_ERR_INVALID_ARG, "models: bad pointer/count");
+    for (int i = 0; i < nmodels; i++) {
+        const vxl_model& m = models[i];
+        if (!m.data || m.sx <= 0 || m.sy <= 0 || m.sz <= 0)
+            return fail(VXL_ERR_INVALID_ARG, "model %d: null data or non-positive size", i);
+        if ((long long)m.sx * m.sy * m.sz > (1ll << 30))
+            return fail(VXL_ERR_OUT_OF_RANGE, "model %d: more than 2^30 voxels", i);
+    }
+    return VXL_OK;
+}
+
+// dirty-region tail of OnUpdate (ShadowVoxSystem.cpp:180-190)
+static void region_from_aabb(const int* aabb, int sx, int sy, int sz, int32_t* region) {
+    if (aabb[3] != 0 || aabb[4] != 0 || aabb[5] != 0) {
+        int mn[3] = {aabb[0] / 2, aabb[1] / 2, aabb[2] / 2};
+        int mx[3] = {aabb[3] / 2, aabb[4] / 2, aabb[5] / 2};
+        int lim[3] = {sx - 1, sy - 1, sz - 1};
+        for (int a = 0; a < 3; a++) {
+            if (mn[a] < 0) mn[a] = 0;
+            if (mx[a] > lim[a]) mx[a] = lim[a];
+            region[a] = mn[a];
+            region[3 + a] = mx[a] - mn[a] + 1;
+        }
+    } else {
+        for (int a = 0; a < 6; a++) region[a] = -1;
+    }
+}
+
+static vxl_status check_params(const vxl_trace_params* p) {
+    if (!p) return fail(VXL_ERR_INVALID_ARG, "params is NULL");
+    if (p->mode != VXL_MODE_DDA) return fail(VXL_ERR_NOT_SUPPORTED, "trace_occlusion: mode must be VXL_MODE_DDA");
+    if (p->n_shadow < 0 || p->n_shadow > 1) return fail(VXL_ERR_INVALID_ARG, "n_shadow must be 0 or 1");
+    if (p->n_ao < 0 || p->n_ao > 64) return fail(VXL_ERR_INVALID_ARG, "n_ao must be in [0,64]");
+    if (p->n_spec < 0 || p->n_spec > 8) return fail(VXL_ERR_INVALID_ARG, "n_spec must be in [0,8]");
+    if (p->n_ao > 0 && !(p->ao_len > 0.0f)) return fail(VXL_ERR_INVALID_ARG, "ao_len must be > 0");
+    return VXL_OK;
+}
+
+}  // namespace vxl
+
+using namespace vxl;
+
+extern "C" {
+
+int vxl_abi_version(void) { return VXL_ABI_VERSION; }
+const char* vxl_last_error_string(void) { return g_last_error.c_str(); }
+const char* vxl_status_string(vxl_status s) {
+    switch (s) {
+        case VXL_OK: return "VXL_OK";
+        case VXL_ERR_INVALID_ARG: return "VXL_ERR_INVALID_ARG";
+        case VXL_ERR_OOM: return "VXL_ERR_OOM";
+        case VXL_ERR_CUDA: return "VXL_ERR_CUDA";
+        case VXL_ERR_TIMEOUT: return "VXL_ERR_TIMEOUT";
+        case VXL_ERR_OUT_OF_RANGE: return "VXL_ERR_OUT_OF_RANGE";
+        case VXL_ERR_IO: return "VXL_ERR_IO";
+        case VXL_ERR_NOT_SUPPORTED: return "VXL_ERR_NOT_SUPPORTED";
+    }
+    return "VXL_ERR_?";
+}
+
+vxl_status vxl_ctx_create(int device, vxl_ctx** out) {
+    if (!out) return fail(VXL_ERR_INVALID_ARG, "ctx_create: out is NULL");
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceCount");
+    if (device < 0 || device >= n) return fail(VXL_ERR_INVALID_ARG, "ctx_create: device %d of %d", device, n);
+    VXL_TRY_CUDA(cudaSetDevice(device));
+    vxl_ctx* c = new (std::nothrow) vxl_ctx();
+    if (!c) return fail(VXL_ERR_OOM, "ctx_create: host allocation");
+    c->device = device;
+    e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) {
+        delete c;
+        return cuda_fail(e, "cudaDeviceGetAttribute");
+    }
+    *out = c;
+    return VXL_OK;
+}
+
+vxl_status vxl_ctx_destroy(vxl_ctx* ctx) {
+    if (!ctx) return VXL_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->d_scratch) cudaFree(ctx->d_scratch);
+    if (ctx->d_stage) cudaFree(ctx->d_stage);
+    delete ctx;
+    return VXL_OK;
+}
+
+vxl_status vxl_ctx_launch_count(const vxl_ctx* ctx, uint64_t* out) {
+    if (!ctx || !out) return fail(VXL_ERR_INVALID_ARG, "ctx_launch_count: NULL argument");
+    *out = ctx->launches;
+    return VXL_OK;
+}
+
+vxl_status vxl_grid_create(vxl_ctx* ctx, int nx, int ny, int nz, vxl_grid** out) {
+    if (!ctx || !out) return fail(VXL_ERR_INVALID_ARG, "grid_create: NULL argument");
+    *out = nullptr;
+    if (nx < 2 || ny < 2 || nz < 2 || (nx & 1) || (ny & 1) || (nz & 1) || nx > 32768 || ny > 32768 || nz > 32768)
+        return fail(VXL_ERR_INVALID_ARG, "grid_create: dims %dx%dx%d must be even and in [2, 32768]", nx, ny, nz);
+    int tx = nx / 8 + 1 + (nx % 8 ? 1 : 0), ty = ny / 8 + 1 + (ny % 8 ? 1 : 0), tz = nz / 8 + 1 + (nz % 8 ? 1 : 0);
+    unsigned long long ntiles = (unsigned long long)tx * ty * tz;
+    if (ntiles * 8ull >= (1ull << 32))
+        return fail(VXL_ERR_OUT_OF_RANGE, "grid_create: %dx%dx%d needs more than 2^32 brick words", nx, ny, nz);
+    VXL_TRY(set_device(ctx));
+    vxl_grid* g = new (std::nothrow) vxl_grid();
+    if (!g) return fail(VXL_ERR_OOM, "grid_create: host allocation");
+    g->ctx = ctx;
+    g->nx = nx;
+    g->ny = ny;
+    g->nz = nz;
+    g->tx = tx;
+    g->ty = ty;
+    g->tz = tz;
+    g->nwords = (size_t)ntiles * 8;
+    g->nmask = (size_t)((ntiles + 31) / 32);
+    cudaError_t e = cudaMalloc(&g->words, g->nwords * sizeof(uint64_t));
+    if (e == cudaSuccess) e = cudaMalloc(&g->tmask, g->nmask * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(g->words, 0, g->nwords * sizeof(uint64_t));
+    if (e == cudaSuccess) e = cudaMemset(g->tmask, 0, g->nmask * sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        if (g->words) cudaFree(g->words);
+        if (g->tmask) cudaFree(g->tmask);
+        delete g;
+        return cuda_fail(e, "grid_create: device allocation");
+    }
+    *out = g;
+    return VXL_OK;
+}
+
+vxl_status vxl_grid_destroy(vxl_grid* g) {
+    if (!g) return VXL_OK;
+    cudaSetDevice(g->ctx->device);
+    cudaFree(g->words);
+    cudaFree(g->tmask);
+    delete g;
+    return VXL_OK;
+}
+
+vxl_status vxl_grid_describe(const vxl_grid* g, vxl_grid_desc* out) {
+    if (!grid_ok(g) || !out) return fail(VXL_ERR_INVALID_ARG, "grid_describe: NULL argument");
+    out->nx = g->nx;
+    out->ny = g->ny;
+    out->nz = g->nz;
+    out->tx = g->tx;
+    out->ty = g->ty;
+    out->tz = g->tz;
+    out->words = g->words;
+    out->words_bytes = g->nwords * sizeof(uint64_t);
+    out->tile_mask = g->tmask;
+    out->tile_mask_bytes = g->nmask * sizeof(uint32_t);
+    return VXL_OK;
+}
+
+vxl_status vxl_grid_clear(vxl_grid* g, void* stream) {
+    if (!grid_ok(g)) return fail(VXL_ERR_INVALID_ARG, "grid_clear: bad grid");
+    VXL_TRY(set_device(g->ctx));
+    VXL_TRY_CUDA(cudaMemsetAsync(g->words, 0, g->nwords * sizeof(uint64_t), (cudaStream_t)stream));
+    VXL_TRY_CUDA(cudaMemsetAsync(g->tmask, 0, g->nmask * sizeof(uint32_t), (cudaStream_t)stream));
+    return VXL_OK;
+}
+
+vxl_status vxl_grid_build_bricks(vxl_grid* g, void* stream) {
+    if (!grid_ok(g)) return fail(VXL_ERR_INVALID_ARG, "grid_build_bricks: bad grid");
+    VXL_TRY(set_device(g->ctx));
+    return launch_build_tile_mask(g, (cudaStream_t)stream);
+}
+
+vxl_status vxl_grid_import_r8(vxl_grid* g, const uint8_t* d_bytes, void* stream) {
+    if (!grid_ok(g) || !d_bytes) return fail(VXL_ERR_INVALID_ARG, "grid_import_r8: NULL argument");
+    VXL_TRY(set_device(g->ctx));
+    return launch_grid_import_r8(g, d_bytes, (cudaStream_t)stream);
+}
+
+vxl_status vxl_grid_export_r8(const vxl_grid* g, uint8_t* d_bytes, void* stream) {
+    if (!grid_ok(g) || !d_bytes) return fail(VXL_ERR_INVALID_ARG, "grid_export_r8: NULL argument");
+    VXL_TRY(set_device(g->ctx));
+    return launch_grid_export_r8(g, d_bytes, (cudaStream_t)stream);
+}
+
+vxl_status vxl_grid_import_palette(vxl_grid* g, const uint8_t* d_palette, int opaque_min, void* stream) {
+    if (!grid_ok(g) || !d_palette) return fail(VXL_ERR_INVALID_ARG, "grid_import_palette: NULL argument");
+    if (opaque_min < 0 || opaque_min > 256) return fail(VXL_ERR_INVALID_ARG, "opaque_min out of [0,256]");
+    VXL_TRY(set_device(g->ctx));
+    return launch_grid_import_palette(g, d_palette, opaque_min, (cudaStream_t)stream);
+}
+
+vxl_status vxl_grid_count(const vxl_grid* g, uint64_t* out, void* stream) {
+    if (!grid_ok(g) || !out) return fail(VXL_ERR_INVALID_ARG, "grid_count: NULL argument");
+    VXL_TRY(set_device(g->ctx));
+    cudaStream_t s = (cudaStream_t)stream;
+    void* scratch;
+    VXL_TRY(ctx_scratch(g->ctx, 256, &scratch));
+    VXL_TRY_CUDA(cudaMemsetAsync(scratch, 0, sizeof(unsigned long long), s));
+    VXL_TRY(launch_grid_count(g, (unsigned long long*)scratch, s));
+    unsigned long long h = 0;
+    VXL_TRY_CUDA(cudaMemcpyAsync(&h, scratch, sizeof h, cudaMemcpyDeviceToHost, s));
+    VXL_TRY_CUDA(cudaStreamSynchronize(s));
+    *out = h;
+    return VXL_OK;
+}
+
+vxl_status vxl_trace_rays(vxl_ctx* ctx, const vxl_grid* g, const float* d_rays, int64_t n, vxl_mode mode,
+                          vxl_ray_record* d_records, void* stream) {
+    if (!ctx || !grid_ok(g) || (n > 0 && (!d_rays || !d_records)))
+        return fail(VXL_ERR_INVALID_ARG, "trace_rays: NULL argument");
+    if (n < 0) return fail(VXL_ERR_INVALID_ARG, "trace_rays: n < 0");
+    if (mode != VXL_MODE_DDA && mode != VXL_MODE_SPARSE && mode != VXL_MODE_SUPERSPARSE)
+        return fail(VXL_ERR_INVALID_ARG, "trace_rays: unknown mode %d", (int)mode);
+    VXL_TRY(set_device(ctx));
+    return launch_trace_rays(ctx, g, d_rays, n, (int)mode, d_records, (cudaStream_t)stream);
+}
+
+vxl_status vxl_trace_occlusion(vxl_ctx* ctx, const vxl_grid* g, const vxl_gbuffer* gb, const vxl_trace_params* p,
+                               const vxl_outputs* out, void* stream) {
+    if (!ctx || !grid_ok(g) || !gb || !out) return fail(VXL_ERR_INVALID_ARG, "trace_occlusion: NULL argument");
+    VXL_TRY(check_params(p));
+    if (gb->npix < 0) return fail(VXL_ERR_INVALID_ARG, "trace_occlusion: npix < 0");
+    if (gb->npix > 0 && (!gb->pos || !gb->nrm)) return fail(VXL_ERR_INVALID_ARG, "trace_occlusion: NULL G-buffer");
+    VXL_TRY(set_device(ctx));
+    return launch_trace_occlusion(ctx, g, gb, p, out, (cudaStream_t)stream);
+}
+
+vxl_status vxl_trace_occlusion_host(vxl_ctx* ctx, const vxl_grid* g, const float* h_pos, const float* h_nrm,
+                                    const float* h_rough, int64_t npix, const vxl_trace_params* p, float* h_shadow,
+                                    float* h_ao, float* h_ao_vis, float* h_spec, float* h_spec_t, void* stream) {
+    if (!ctx || !grid_ok(g)) return fail(VXL_ERR_INVALID_ARG, "trace_occlusion_host: NULL argument");
+    VXL_TRY(check_params(p));
+    if (npix < 0 || (npix > 0 && (!h_pos || !h_nrm))) return fail(VXL_ERR_INVALID_ARG, "trace_occlusion_host: bad G-buffer");
+    if (npix == 0) return VXL_OK;
+    VXL_TRY(set_device(ctx));
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t b3 = (size_t)npix * 3 * sizeof(float), b1 = (size_t)npix * sizeof(float);
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    size_t need = 2 * al(b3) + 6 * al(b1);
+    void* st;
+    VXL_TRY(ctx_stage(ctx, need, &st));
+    char* base = (char*)st;
+    float* d_pos = (float*)base;
+    float* d_nrm = (float*)(base + al(b3));
+    float* d_rough = (float*)(base + 2 * al(b3));
+    float* outs[5];
+    for (int k = 0; k < 5; k++) outs[k] = (float*)(base + 2 * al(b3) + (k + 1) * al(b1));
+    VXL_TRY_CUDA(cudaMemcpyAsync(d_pos, h_pos, b3, cudaMemcpyHostToDevice, s));
+    VXL_TRY_CUDA(cudaMemcpyAsync(d_nrm, h_nrm, b3, cudaMemcpyHostToDevice, s));
+    if (h_rough) VXL_TRY_CUDA(cudaMemcpyAsync(d_rough, h_rough, b1, cudaMemcpyHostToDevice, s));
+    vxl_gbuffer gb{d_pos, d_nrm, h_rough ? d_rough : nullptr, npix, 0, 0};
+    float* hs[5] = {h_shadow, h_ao, h_ao_vis, h_spec, h_spec_t};
+    vxl_outputs o{hs[0] ? outs[0] : nullptr, hs[1] ? outs[1] : nullptr, hs[2] ? outs[2] : nullptr,
+                  hs[3] ? outs[3] : nullptr, hs[4] ? outs[4] : nullptr, nullptr};
+    VXL_TRY(launch_trace_occlusion(ctx, g, &gb, p, &o, s));
+    for (int k = 0; k < 5; k++)
+        if (hs[k]) VXL_TRY_CUDA(cudaMemcpyAsync(hs[k], outs[k], b1, cudaMemcpyDeviceToHost, s));
+    VXL_TRY_CUDA(cudaStreamSynchronize(s));
+    return VXL_OK;
+}
+
+vxl_status vxl_light_ambient(vxl_ctx* ctx, const vxl_grid* g, const float* d_wcp, const float* d_nrm,
+                             const float* d_depth, const float* d_noise, int64_t npix, float* d_shadow,
+                             float* d_irradiance, vxl_ray_record* d_records, void* stream) {
+    if (!ctx || !grid_ok(g) || npix < 0) return fail(VXL_ERR_INVALID_ARG, "light_ambient: bad argument");
+    if (npix > 0 && (!d_wcp || !d_nrm || !d_depth || !d_noise || !d_shadow || !d_irradiance))
+        return fail(VXL_ERR_INVALID_ARG, "light_ambient: NULL buffer");
+    VXL_TRY(set_device(ctx));
+    return launch_light_ambient(ctx, g, d_wcp, d_nrm, d_depth, d_noise, npix, d_shadow, d_irradiance, d_records,
+                                (cudaStream_t)stream);
+}
+
+vxl_status vxl_light_reflection(vxl_ctx* ctx, const vxl_grid* g, const float* d_wcp, const float* d_nrm,
+                                const float* d_view_r, const float* d_rough, const float* d_noise, int64_t npix,
+                                float* d_t, vxl_ray_record* d_records, void* stream) {
+    if (!ctx || !grid_ok(g) || npix < 0) return fail(VXL_ERR_INVALID_ARG, "light_reflection: bad argument");
+    if (npix > 0 && (!d_wcp || !d_nrm || !d_view_r || !d_rough || !d_noise || !d_t))
+        return fail(VXL_ERR_INVALID_ARG, "light_reflection: NULL buffer");
+    VXL_TRY(set_device(ctx));
+    return launch_light_reflection(ctx, g, d_wcp, d_nrm, d_view_r, d_rough, d_noise, npix, d_t, d_records,
+                                   (cudaStream_t)stream);
+}
+
+vxl_status vxl_light_point(vxl_ctx* ctx, const vxl_grid* g, const float* d_wpos, const float* d_nrm,
+                           const float* d_noise, int64_t npix, const float light_pos[3], float range, int spot,
+                           float* d_shadow, vxl_ray_record* d_records, void* stream) {
+    if (!ctx || !grid_ok(g) || npix < 0 || !light_pos) return fail(VXL_ERR_INVALID_ARG, "light_point: bad argument");
+    if (npix > 0 && (!d_wpos || !d_nrm || !d_noise || !d_shadow))
+        return fail(VXL_ERR_INVALID_ARG, "light_point: NULL buffer");
+    VXL_TRY(set_device(ctx));
+    return launch_light_point(ctx, g, d_wpos, d_nrm, d_noise, npix, light_pos, range, spot ? 1 : 0, d_shadow,
+                              d_records, (cudaStream_t)stream);
+}
+
+vxl_status vxl_voxelize(vxl_ctx* ctx, vxl_grid* g, const vxl_model* models, int nmodels,
+                        const vxl_instance* instances, int n, int32_t* d_aabb, void* stream) {
+    if (!ctx || !grid_ok(g) || n < 0 || (n > 0 && !instances)) return fail(VXL_ERR_INVALID_ARG, "voxelize: bad argument");
+    VXL_TRY(check_models(models, nmodels));
+    std::vector<DevInstance> inst((size_t)n);
+    for (int i = 0; i < n; i++) {
+        const vxl_instance& a = instances[i];
+        if (a.model < 0 || a.model >= nmodels) return fail(VXL_ERR_INVALID_ARG, "instance %d: model %d of %d", i, a.model, nmodels);
+        if (a.op != VXL_OP_SET && a.op != VXL_OP_CLEAR) return fail(VXL_ERR_INVALID_ARG, "instance %d: bad op", i);
+        std::memcpy(inst[i].m, a.matrix, sizeof inst[i].m);
+        inst[i].model = a.model;
+        inst[i].op = a.op;
+    }
+    VXL_TRY(set_device(ctx));
+    return voxelize_runs(ctx, g, models, nmodels, inst, d_aabb, (cudaStream_t)stream);
+}
+
+vxl_status vxl_shadowvox_update(vxl_ctx* ctx, vxl_grid* g, const vxl_model* models, int nmodels,
+                                const vxl_entity* ents, int n, int32_t* h_regions, void* stream) {
+    if (!ctx || !grid_ok(g) || n < 0 || (n > 0 && !ents)) return fail(VXL_ERR_INVALID_ARG, "shadowvox_update: bad argument");
+    VXL_TRY(check_models(models, nmodels));
+    if (n == 0) return VXL_OK;
+    std::vector<DevInstance> inst((size_t)2 * n);
+    for (int e = 0; e < n; e++) {
+        const vxl_entity& E = ents[e];
+        if (E.model < 0 || E.model >= nmodels) return fail(VXL_ERR_INVALID_ARG, "entity %d: model %d of %d", e, E.model, nmodels);
+        float np[3] = {-E.pivot[0], -E.pivot[1], -E.pivot[2]};
+        translate(E.prev_world, np, inst[2 * e].m);
+        inst[2 * e].model = E.model;
+        inst[2 * e].op = VXL_OP_CLEAR;
+        translate(E.world, np, inst[2 * e + 1].m);
+        inst[2 * e + 1].model = E.model;
+        inst[2 * e + 1].op = VXL_OP_SET;
+    }
+    VXL_TRY(set_device(ctx));
+    cudaStream_t s = (cudaStream_t)stream;
+    const int sx = g->nx / 2, sy = g->ny / 2, sz = g->nz / 2;
+    // per-instance aabb, started at (S-1,S-1,S-1)/(0,0,0) (ShadowVoxSystem.cpp:128-132);
+    // the two instances of an entity are folded together on the host
+    std::vector<int32_t> h_aabb((size_t)12 * n);
+    for (int k = 0; k < 2 * n; k++) {
+        int32_t* a = &h_aabb[(size_t)6 * k];
+        a[0] = sx - 1;
+        a[1] = sy - 1;
+        a[2] = sz - 1;
+        a[3] = a[4] = a[5] = 0;
+    }
+    void* st;
+    VXL_TRY(ctx_stage(ctx, h_aabb.size() * sizeof(int32_t), &st));
+    VXL_TRY_CUDA(cudaMemcpyAsync(st, h_aabb.data(), h_aabb.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    VXL_TRY(voxelize_runs(ctx, g, models, nmodels, inst, (int32_t*)st, s));
+    VXL_TRY_CUDA(cudaMemcpyAsync(h_aabb.data(), st, h_aabb.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    VXL_TRY_CUDA(cudaStreamSynchronize(s));
+    if (h_regions) {
+        for (int e = 0; e < n; e++) {
+            const int32_t* a = &h_aabb[(size_t)12 * e];
+            const int32_t* b = a + 6;
+            int m[6];
+            for (int c = 0; c < 3; c++) {
+                m[c] = a[c] < b[c] ? a[c] : b[c];
+                m[3 + c] = a[3 + c] > b[3 + c] ? a[3 + c] : b[3 + c];
+            }
+            region_from_aabb(m, sx, sy, sz, h_regions + 6 * (size_t)e);
+        }
+    }
+    return VXL_OK;
+}
+
+vxl_status vxl_vox_destroyed(vxl_ctx* ctx, vxl_grid* g, const vxl_model* model, const float world[16],
+                             int32_t* h_region, void* stream) {
+    if (!ctx || !grid_ok(g) || !model || !world) return fail(VXL_ERR_INVALID_ARG, "vox_destroyed: NULL argument");
+    VXL_TRY(check_models(model, 1));
+    VXL_TRY(set_device(ctx));
+    cudaStream_t s = (cudaStream_t)stream;
+    const int sx = g->nx / 2, sy = g->ny / 2, sz = g->nz / 2;
+    std::vector<DevInstance> inst(1);
+    std::memcpy(inst[0].m, world, sizeof inst[0].m);
+    inst[0].model = 0;
+    inst[0].op = VXL_OP_CLEAR;
+    int32_t h_aabb[6] = {sx - 1, sy - 1, sz - 1, 0, 0, 0};
+    void* st;
+    VXL_TRY(ctx_stage(ctx, sizeof h_aabb, &st));
+    VXL_TRY_CUDA(cudaMemcpyAsync(st, h_aabb, sizeof h_aabb, cudaMemcpyHostToDevice, s));
+    VXL_TRY(voxelize_runs(ctx, g, model, 1, inst, (int32_t*)st, s));
+    VXL_TRY_CUDA(cudaMemcpyAsync(h_aabb, st, sizeof h_aabb, cudaMemcpyDeviceToHost, s));
+    VXL_TRY_CUDA(cudaStreamSynchronize(s));
+    if (h_region) region_from_aabb(h_aabb, sx, sy, sz, h_region);
+    return VXL_OK;
+}
+
+vxl_status vxl_read_v(const char* path, int32_t* sx, int32_t* sy, int32_t* sz, uint8_t* h_data, size_t capacity) {
+    if (!path || !sx || !sy || !sz) return fail(VXL_ERR_INVALID_ARG, "read_v: NULL argument");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(VXL_ERR_IO, "read_v: cannot open %s", path);
+    uint32_t d[3];
+    if (std::fread(d, sizeof(uint32_t), 3, f) != 3) {
+        std::fclose(f);
+        return fail(VXL_ERR_IO, "read_v: %s: truncated header", path);
+    }
+    if (d[0] == 0 || d[1] == 0 || d[2] == 0 || (unsigned long long)d[0] * d[1] * d[2] > (1ull << 30)) {
+        std::fclose(f);
+        return fail(VXL_ERR_IO, "read_v: %s: implausible size %ux%ux%u", path, d[0], d[1], d[2]);
+    }
+    *sx = (int32_t)d[0];
+    *sy = (int32_t)d[1];
+    *sz = (int32_t)d[2];
+    size_t n = (size_t)d[0] * d[1] * d[2];
+    if (!h_data) {
+        std::fclose(f);
+        return VXL_OK;
+    }
+    if (capacity < n) {
+        std::fclose(f);
+        return fail(VXL_ERR_INVALID_ARG, "read_v: capacity %zu < %zu", capacity, n);
+    }
+    size_t got = std::fread(h_data, 1, n, f);
+    std::fclose(f);
+    if (got != n) return fail(VXL_ERR_IO, "read_v: %s: truncated body (%zu of %zu bytes)", path, got, n);
+    return VXL_OK;
+}
+
+vxl_status vxl_scene_noise(vxl_ctx* ctx, vxl_grid* g, uint32_t seed, float thresh, float freq, int ground_y,
+                           void* stream) {
+    if (!ctx || !grid_ok(g)) return fail(VXL_ERR_INVALID_ARG, "scene_noise: bad argument");
+    VXL_TRY(set_device(ctx));
+    return launch_scene_noise(g, seed, thresh, freq, ground_y, (cudaStream_t)stream);
+}
+
+vxl_status vxl_scene_boxes(vxl_ctx* ctx, vxl_grid* g, uint32_t seed, int nboxes, int smin, int smax, void* stream) {
+    if (!ctx || !grid_ok(g) || nboxes < 0 || smin < 1 || smax < smin)
+        return fail(VXL_ERR_INVALID_ARG, "scene_boxes: bad argument");
+    VXL_TRY(set_device(ctx));
+    return launch_scene_boxes(g, seed, nboxes, smin, smax, (cudaStream_t)stream);
+}
+
+vxl_status vxl_scene_gbuffer(vxl_ctx* ctx, const vxl_grid* g, const float cam[3], const float target[3],
+                             float tan_half_fov, int W, int H, uint32_t seed, float* d_pos, float* d_nrm,
+                             float* d_rough, void* stream) {
+    if (!ctx || !grid_ok(g) || !cam || !target || W <= 0 || H <= 0 || !d_pos || !d_nrm || !d_rough)
+        return fail(VXL_ERR_INVALID_ARG, "scene_gbuffer: bad argument");
+    VXL_TRY(set_device(ctx));
+    return launch_scene_gbuffer(g, cam, target, tan_half_fov, W, H, seed, d_pos, d_nrm, d_rough, (cudaStream_t)stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,95 @@
+// vxl_internal.h — library-internal declarations shared by the host API
+// (vxl_api.cpp) and the kernel translation units (*.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "../../include/vxl.h"
+
+struct vxl_ctx {
+    int device;
+    int sm_count;
+    uint64_t launches;
+    // growable device scratch (voxelizer tables, host-API staging, counters)
+    void* d_scratch;
+    size_t d_scratch_bytes;
+    void* d_stage;
+    size_t d_stage_bytes;
+};
+
+struct vxl_grid {
+    vxl_ctx* ctx;
+    int nx, ny, nz;
+    int tx, ty, tz;
+    uint64_t* words;
+    size_t nwords;
+    uint32_t* tmask;
+    size_t nmask;  // uint32 words of the tile mask
+};
+
+namespace vxl {
+
+// error plumbing (vxl_api.cpp)
+vxl_status fail(vxl_status s, const char* fmt, ...);
+vxl_status cuda_fail(cudaError_t e, const char* what);
+#define VXL_TRY_CUDA(expr)                                      \
+    do {                                                        \
+        cudaError_t e_ = (expr);                                \
+        if (e_ != cudaSuccess) return ::vxl::cuda_fail(e_, #expr); \
+    } while (0)
+#define VXL_TRY(expr)                       \
+    do {                                    \
+        vxl_status s_ = (expr);             \
+        if (s_ != VXL_OK) return s_;        \
+    } while (0)
+
+// device scratch owned by the context (grows, never shrinks)
+vxl_status ctx_scratch(vxl_ctx* ctx, size_t bytes, void** out);
+vxl_status ctx_stage(vxl_ctx* ctx, size_t bytes, void** out);
+
+struct DevInstance {
+    float m[16];
+    int32_t model;
+    int32_t op;
+};
+struct DevModel {
+    const uint8_t* data;
+    int32_t sx, sy, sz;
+    int32_t pad;
+};
+
+// launchers (kernels in grid.cu / trace.cu / voxelize.cu); each returns the
+// launch error and counts launches in ctx
+vxl_status launch_grid_import_r8(vxl_grid* g, const uint8_t* bytes, cudaStream_t s);
+vxl_status launch_grid_export_r8(const vxl_grid* g, uint8_t* bytes, cudaStream_t s);
+vxl_status launch_grid_import_palette(vxl_grid* g, const uint8_t* pal, int opaque_min, cudaStream_t s);
+vxl_status launch_build_tile_mask(vxl_grid* g, cudaStream_t s);
+vxl_status launch_grid_count(const vxl_grid* g, unsigned long long* d_out, cudaStream_t s);
+vxl_status launch_scene_noise(vxl_grid* g, uint32_t seed, float thresh, float freq, int ground_y, cudaStream_t s);
+vxl_status launch_scene_boxes(vxl_grid* g, uint32_t seed, int nboxes, int smin, int smax, cudaStream_t s);
+vxl_status launch_scene_gbuffer(const vxl_grid* g, const float cam[3], const float target[3], float tan_half_fov,
+                                int W, int H, uint32_t seed, float* pos, float* nrm, float* rough, cudaStream_t s);
+
+vxl_status launch_trace_rays(vxl_ctx* ctx, const vxl_grid* g, const float* rays, int64_t n, int mode,
+                             vxl_ray_record* rec, cudaStream_t s);
+vxl_status launch_trace_occlusion(vxl_ctx* ctx, const vxl_grid* g, const vxl_gbuffer* gb, const vxl_trace_params* p,
+                                  const vxl_outputs* out, cudaStream_t s);
+vxl_status launch_light_ambient(vxl_ctx* ctx, const vxl_grid* g, const float* wcp, const float* nrm,
+                                const float* depth, const float* noise, int64_t npix, float* shadow, float* irr,
+                                vxl_ray_record* rec, cudaStream_t s);
+vxl_status launch_light_reflection(vxl_ctx* ctx, const vxl_grid* g, const float* wcp, const float* nrm,
+                                   const float* view_r, const float* rough, const float* noise, int64_t npix,
+                                   float* t, vxl_ray_record* rec, cudaStream_t s);
+vxl_status launch_light_point(vxl_ctx* ctx, const vxl_grid* g, const float* wpos, const float* nrm,
+                              const float* noise, int64_t npix, const float lp[3], float range, int spot,
+                              float* shadow, vxl_ray_record* rec, cudaStream_t s);
+
+// one pass of instances that all carry the same op (they commute)
+vxl_status launch_voxelize_run(vxl_grid* g, const DevInstance* d_inst, const DevModel* d_models,
+                               const int2* d_chunks, int nchunks, int value, int32_t* d_aabb, cudaStream_t s);
+
+constexpr int kVoxChunk = 1024;  // source voxels per voxelizer block
+
+}  // namespace vxl
