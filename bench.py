@@ -230,6 +230,8 @@ def run_gpu(args, wl):
     torch.cuda.set_device(local)
     V.build()
     ctx = V.Context(local)
+    if args.tuning:
+        ctx.set_tuning(*[int(x) for x in args.tuning.split(",")])
     n, W, H = wl["n"], wl["W"], wl["H"]
     npix = W * H
     R = wl["n_shadow"] + wl["n_ao"] + wl["n_spec"]
@@ -326,6 +328,7 @@ def run_gpu(args, wl):
         "e2e": {"value": e2e, "unit": "Grays/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "vxl_trace_occlusion_host, pinned host G-buffer and outputs"},
         "gpu_launches": int(launches),
+        "tuning": ctx.get_tuning(),
         "clocks": clk.summary(),
     }
     if not args.no_cpu_baseline:
@@ -356,6 +359,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--tuning", default="", help="tile_px,kstep,leap,order for the occlusion kernel")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":

@@ -54,16 +54,30 @@ vxl_status vxl_ctx_destroy(vxl_ctx* ctx);
 /* number of kernels this library launched through ctx (diagnostics) */
 vxl_status vxl_ctx_launch_count(const vxl_ctx* ctx, uint64_t* out);
 
+/* Launch-shape knobs of the occlusion kernel (results do not depend on them).
+ * Zero fields keep the current value. Picked per device by the autotuner
+ * (voxelengine_gb300/autotune.py). */
+typedef struct vxl_tuning {
+    int32_t tile_px;   /* pixels per warp tile: 16 or 32 */
+    int32_t kstep;     /* DDA iterations between pool refills: 1, 2, 4 or 8 */
+    int32_t leap;      /* 1: cross empty bricks in one step where exact; 2: never */
+    int32_t order;     /* 1: dispatch spec, shadow, AO; 2: shadow, AO, spec */
+} vxl_tuning;
+vxl_status vxl_ctx_set_tuning(vxl_ctx* ctx, const vxl_tuning* t);
+vxl_status vxl_ctx_get_tuning(const vxl_ctx* ctx, vxl_tuning* out);
+
 /* ------------------------------------------------------------------ grid
  * Replaces ShadowVoxSystem's R8Uint volume (ShadowVoxSystem.cpp:55-79,
  * ShadowVoxSystem.h:29 GetVolumeImage). Storage: 1 bit per fine voxel in
- * 4x4x4 bricks (one uint64 each), 8 bricks per 8^3 tile (64 bytes), tiles in
- * x-fastest order, plus one zero tile of padding on the + side of every axis.
+ * 4x4x4 bricks, one uint64 each (bit (x&3) + 4*(y&3) + 16*(z&3)), bricks in
+ * x-fastest order, plus one zero brick of padding on the + side of every
+ * axis; and a tile map with 1 bit per 8^3 tile (2x2x2 bricks), x-fastest.
  * nx, ny, nz must be even and in [2, 32768]. */
 typedef struct vxl_grid_desc {
     int32_t nx, ny, nz;        /* fine dimensions */
-    int32_t tx, ty, tz;        /* tiles per axis, padding included */
-    uint64_t* words;           /* device: tx*ty*tz*8 uint64 */
+    int32_t bx, by, bz;        /* 4^3 bricks per axis, padding included */
+    int32_t tx, ty, tz;        /* 8^3 tiles per axis */
+    uint64_t* words;           /* device: bx*by*bz uint64 */
     size_t words_bytes;
     uint32_t* tile_mask;       /* device: 1 bit per tile, "tile has any voxel set" */
     size_t tile_mask_bytes;

@@ -32,7 +32,7 @@ REC_BYTES = 24
 # every symbol include/vxl.h declares
 EXPORTED = [
     "vxl_abi_version", "vxl_last_error_string", "vxl_status_string", "vxl_ctx_create", "vxl_ctx_destroy",
-    "vxl_ctx_launch_count", "vxl_grid_create", "vxl_grid_destroy", "vxl_grid_describe", "vxl_grid_clear",
+    "vxl_ctx_launch_count", "vxl_ctx_set_tuning", "vxl_ctx_get_tuning", "vxl_grid_create", "vxl_grid_destroy", "vxl_grid_describe", "vxl_grid_clear",
     "vxl_grid_build_bricks", "vxl_grid_import_r8", "vxl_grid_export_r8", "vxl_grid_import_palette",
     "vxl_grid_count", "vxl_trace_rays", "vxl_trace_occlusion", "vxl_trace_occlusion_host", "vxl_light_ambient",
     "vxl_light_reflection", "vxl_light_point", "vxl_voxelize", "vxl_shadowvox_update", "vxl_vox_destroyed",
@@ -47,9 +47,9 @@ class VxlError(RuntimeError):
 
 
 class GridDesc(C.Structure):
-    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("tx", C.c_int32), ("ty", C.c_int32),
-                ("tz", C.c_int32), ("words", C.c_void_p), ("words_bytes", C.c_size_t), ("tile_mask", C.c_void_p),
-                ("tile_mask_bytes", C.c_size_t)]
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("bx", C.c_int32), ("by", C.c_int32),
+                ("bz", C.c_int32), ("tx", C.c_int32), ("ty", C.c_int32), ("tz", C.c_int32), ("words", C.c_void_p),
+                ("words_bytes", C.c_size_t), ("tile_mask", C.c_void_p), ("tile_mask_bytes", C.c_size_t)]
 
 
 class GBuffer(C.Structure):
@@ -67,6 +67,13 @@ class TraceParams(C.Structure):
 class Outputs(C.Structure):
     _fields_ = [("shadow", C.c_void_p), ("ao", C.c_void_p), ("ao_vis", C.c_void_p), ("spec", C.c_void_p),
                 ("spec_t", C.c_void_p), ("records", C.c_void_p)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("tile_px", C.c_int32), ("kstep", C.c_int32), ("leap", C.c_int32), ("order", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class Model(C.Structure):
@@ -87,7 +94,7 @@ _lock = threading.Lock()
 
 
 def build(force: bool = False) -> str:
-    from . import build as _b
+    from . import buildlib as _b
 
     return _b.build(force=force)
 
@@ -109,6 +116,8 @@ def lib():
         L.vxl_ctx_create.argtypes = [C.c_int, C.POINTER(vp)]
         L.vxl_ctx_destroy.argtypes = [vp]
         L.vxl_ctx_launch_count.argtypes = [vp, C.POINTER(C.c_uint64)]
+        L.vxl_ctx_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
+        L.vxl_ctx_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
         L.vxl_grid_create.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(vp)]
         L.vxl_grid_destroy.argtypes = [vp]
         L.vxl_grid_describe.argtypes = [vp, C.POINTER(GridDesc)]
@@ -187,6 +196,15 @@ class Context:
         n = C.c_uint64()
         check(lib().vxl_ctx_launch_count(self._h, C.byref(n)))
         return n.value
+
+    def set_tuning(self, tile_px=0, kstep=0, leap=0, order=0):
+        t = Tuning(tile_px, kstep, leap, order)
+        check(lib().vxl_ctx_set_tuning(self._h, C.byref(t)))
+
+    def get_tuning(self) -> dict:
+        t = Tuning()
+        check(lib().vxl_ctx_get_tuning(self._h, C.byref(t)))
+        return t.as_dict()
 
     def close(self):
         if self._h:

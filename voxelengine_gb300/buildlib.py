@@ -48,7 +48,7 @@ def up_to_date() -> bool:
 
 def _compile(src: str, verbose: bool) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-    cmd = [nvcc()] + ARCH + CU_FLAGS + ["-I", INCLUDE, "-c", src, "-o", obj]
+    cmd = [nvcc()] + ARCH + CU_FLAGS + os.environ.get("VXL_NVCC_EXTRA", "").split() + ["-I", INCLUDE, "-c", src, "-o", obj]
     if src.endswith(".cpp"):
         cmd = [nvcc(), "-O2", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-x", "c++",
                "-I", INCLUDE, "-c", src, "-o", obj]

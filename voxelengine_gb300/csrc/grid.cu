@@ -4,28 +4,13 @@
 
 namespace vxl {
 
-static GridView view_of(const vxl_grid* g) {
-    GridView v;
-    v.words = g->words;
-    v.tmask = g->tmask;
-    v.nx = g->nx;
-    v.ny = g->ny;
-    v.nz = g->nz;
-    v.tx = g->tx;
-    v.ty = g->ty;
-    v.tz = g->tz;
-    v.txy = (uint32_t)g->tx * (uint32_t)g->ty;
-    return v;
-}
-
 // fine coordinates of bit b of word w (inverse of word_index / bit_index)
 __device__ __forceinline__ void word_origin(const GridView& g, uint32_t w, int* x0, int* y0, int* z0) {
-    uint32_t tile = w >> 3, sub = w & 7u;
-    uint32_t tz = tile / g.txy, rem = tile - tz * g.txy;
-    uint32_t ty = rem / (uint32_t)g.tx, tx = rem - ty * (uint32_t)g.tx;
-    *x0 = (int)(tx * 8u + (sub & 1u) * 4u);
-    *y0 = (int)(ty * 8u + ((sub >> 1) & 1u) * 4u);
-    *z0 = (int)(tz * 8u + ((sub >> 2) & 1u) * 4u);
+    uint32_t bz = w / g.bxy, rem = w - bz * g.bxy;
+    uint32_t by = rem / (uint32_t)g.bx, bx = rem - by * (uint32_t)g.bx;
+    *x0 = (int)(bx * 4u);
+    *y0 = (int)(by * 4u);
+    *z0 = (int)(bz * 4u);
 }
 
 // ---------------------------------------------------------------- R8 in/out
@@ -89,15 +74,18 @@ __global__ void k_import_palette(GridView g, uint64_t* words, const uint8_t* __r
     words[w] = out;
 }
 
-// one bit per 8^3 tile: any of its 8 words non-zero
-__global__ void k_tile_mask(const uint64_t* __restrict__ words, uint32_t* mask, uint32_t ntiles, uint32_t nmask) {
+// one bit per 8^3 tile: any of its 2x2x2 bricks non-zero
+__global__ void k_tile_mask(GridView g, uint32_t* mask, int by_, int bz_, uint32_t ntiles, uint32_t nmask) {
     uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nmask * 32u) return;
     bool any = false;
     if (t < ntiles) {
-        const ulonglong2* p = reinterpret_cast<const ulonglong2*>(words + (size_t)t * 8u);
-        ulonglong2 a = p[0], b = p[1], c = p[2], d = p[3];
-        any = (a.x | a.y | b.x | b.y | c.x | c.y | d.x | d.y) != 0ull;
+        uint32_t tz = t / g.txy, rem = t - tz * g.txy;
+        uint32_t ty = rem / (uint32_t)g.tx, tx = rem - ty * (uint32_t)g.tx;
+        for (int k = 0; k < 8 && !any; k++) {
+            int bx = 2 * tx + (k & 1), by = 2 * ty + ((k >> 1) & 1), bz = 2 * tz + ((k >> 2) & 1);
+            if (bx < g.bx && by < by_ && bz < bz_) any = g.words[(uint32_t)bx + (uint32_t)by * g.bx + bz * g.bxy] != 0ull;
+        }
     }
     unsigned m = __ballot_sync(0xffffffffu, any);
     if ((threadIdx.x & 31) == 0) mask[t >> 5] = m;
@@ -308,8 +296,9 @@ vxl_status launch_grid_import_palette(vxl_grid* g, const uint8_t* pal, int opaqu
 }
 
 vxl_status launch_build_tile_mask(vxl_grid* g, cudaStream_t s) {
-    uint32_t ntiles = (uint32_t)(g->nwords / 8);
-    k_tile_mask<<<blocks_for(g->nmask * 32, 256), 256, 0, s>>>(g->words, g->tmask, ntiles, (uint32_t)g->nmask);
+    uint32_t ntiles = (uint32_t)((size_t)g->tx * g->ty * g->tz);
+    k_tile_mask<<<blocks_for(g->nmask * 32, 256), 256, 0, s>>>(view_of(g), g->tmask, g->by, g->bz, ntiles,
+                                                             (uint32_t)g->nmask);
     g->ctx->launches++;
     VXL_TRY_CUDA(cudaGetLastError());
     return VXL_OK;

@@ -5,20 +5,6 @@
 
 namespace vxl {
 
-static GridView view_of(const vxl_grid* g) {
-    GridView v;
-    v.words = g->words;
-    v.tmask = g->tmask;
-    v.nx = g->nx;
-    v.ny = g->ny;
-    v.nz = g->nz;
-    v.tx = g->tx;
-    v.ty = g->ty;
-    v.tz = g->tz;
-    v.txy = (uint32_t)g->tx * (uint32_t)g->ty;
-    return v;
-}
-
 // ------------------------------------------------------------ ray batches
 template <int MODE>
 __global__ void __launch_bounds__(128) k_trace_rays(GridView g, const float* __restrict__ rays, int64_t n,
@@ -249,6 +235,8 @@ vxl_status launch_trace_rays(vxl_ctx* ctx, const vxl_grid* g, const float* rays,
 vxl_status launch_trace_occlusion(vxl_ctx* ctx, const vxl_grid* g, const vxl_gbuffer* gb, const vxl_trace_params* p,
                                   const vxl_outputs* out, cudaStream_t s) {
     if (gb->npix <= 0) return VXL_OK;
+    if (occl_pool_supported(g, p))
+        return launch_trace_occlusion_pool(ctx, g, gb, p, out, ctx_next_counter(ctx), ctx->tune, s);
     GridView v = view_of(g);
     TraceConsts c;
     c.light = mk(p->light_dir[0], p->light_dir[1], p->light_dir[2]);

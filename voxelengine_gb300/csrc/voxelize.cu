@@ -9,20 +9,6 @@
 
 namespace vxl {
 
-static GridView view_of(const vxl_grid* g) {
-    GridView v;
-    v.words = g->words;
-    v.tmask = g->tmask;
-    v.nx = g->nx;
-    v.ny = g->ny;
-    v.nz = g->nz;
-    v.tx = g->tx;
-    v.ty = g->ty;
-    v.tz = g->tz;
-    v.txy = (uint32_t)g->tx * (uint32_t)g->ty;
-    return v;
-}
-
 // One block per chunk (instance, first source voxel) of kVoxChunk voxels.
 __global__ void __launch_bounds__(256) k_voxelize(GridView g, unsigned long long* words,
                                                   const DevInstance* __restrict__ inst,

@@ -4,6 +4,7 @@
 // host-side matrix arithmetic (glm::translate) matches the reference bit for bit.
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -53,6 +54,8 @@ vxl_status ctx_stage(vxl_ctx* ctx, size_t bytes, void** out) {
     *out = ctx->d_stage;
     return VXL_OK;
 }
+
+int* ctx_next_counter(vxl_ctx* ctx) { return ctx->d_counters + (ctx->counter_next++ % kCounterRing); }
 
 // glm::translate(m, v): Result[3] = m[0]*v[0] + m[1]*v[1] + m[2]*v[2] + m[3]
 static void translate(const float* m, const float* v, float* out) {
@@ -190,10 +193,14 @@ vxl_status vxl_ctx_create(int device, vxl_ctx** out) {
     if (!c) return fail(VXL_ERR_OOM, "ctx_create: host allocation");
     c->device = device;
     e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_counters, kCounterRing * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(c->d_counters, 0, kCounterRing * sizeof(int));
     if (e != cudaSuccess) {
+        if (c->d_counters) cudaFree(c->d_counters);
         delete c;
-        return cuda_fail(e, "cudaDeviceGetAttribute");
+        return cuda_fail(e, "ctx_create");
     }
+    c->tune = vxl_tuning{16, 8, 2, 1};  // best on GB300 for the 512^3 / 1080p workload
     *out = c;
     return VXL_OK;
 }
@@ -203,6 +210,7 @@ vxl_status vxl_ctx_destroy(vxl_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->d_scratch) cudaFree(ctx->d_scratch);
     if (ctx->d_stage) cudaFree(ctx->d_stage);
+    if (ctx->d_counters) cudaFree(ctx->d_counters);
     delete ctx;
     return VXL_OK;
 }
@@ -213,14 +221,47 @@ vxl_status vxl_ctx_launch_count(const vxl_ctx* ctx, uint64_t* out) {
     return VXL_OK;
 }
 
+vxl_status vxl_ctx_set_tuning(vxl_ctx* ctx, const vxl_tuning* t) {
+    if (!ctx || !t) return fail(VXL_ERR_INVALID_ARG, "ctx_set_tuning: NULL argument");
+    vxl_tuning n = ctx->tune;
+    if (t->tile_px) {
+        if (t->tile_px != 16 && t->tile_px != 32) return fail(VXL_ERR_INVALID_ARG, "tile_px must be 16 or 32");
+        n.tile_px = t->tile_px;
+    }
+    if (t->kstep) {
+        if (t->kstep != 1 && t->kstep != 2 && t->kstep != 4 && t->kstep != 8)
+            return fail(VXL_ERR_INVALID_ARG, "kstep must be 1, 2, 4 or 8");
+        n.kstep = t->kstep;
+    }
+    if (t->leap) {
+        if (t->leap != 1 && t->leap != 2) return fail(VXL_ERR_INVALID_ARG, "leap must be 1 or 2");
+        n.leap = t->leap;
+    }
+    if (t->order) {
+        if (t->order != 1 && t->order != 2) return fail(VXL_ERR_INVALID_ARG, "order must be 1 or 2");
+        n.order = t->order;
+    }
+    ctx->tune = n;
+    return VXL_OK;
+}
+
+vxl_status vxl_ctx_get_tuning(const vxl_ctx* ctx, vxl_tuning* out) {
+    if (!ctx || !out) return fail(VXL_ERR_INVALID_ARG, "ctx_get_tuning: NULL argument");
+    *out = ctx->tune;
+    return VXL_OK;
+}
+
 vxl_status vxl_grid_create(vxl_ctx* ctx, int nx, int ny, int nz, vxl_grid** out) {
     if (!ctx || !out) return fail(VXL_ERR_INVALID_ARG, "grid_create: NULL argument");
     *out = nullptr;
     if (nx < 2 || ny < 2 || nz < 2 || (nx & 1) || (ny & 1) || (nz & 1) || nx > 32768 || ny > 32768 || nz > 32768)
         return fail(VXL_ERR_INVALID_ARG, "grid_create: dims %dx%dx%d must be even and in [2, 32768]", nx, ny, nz);
-    int tx = nx / 8 + 1 + (nx % 8 ? 1 : 0), ty = ny / 8 + 1 + (ny % 8 ? 1 : 0), tz = nz / 8 + 1 + (nz % 8 ? 1 : 0);
+    // bricks cover cells [0, n+1] (the DDA's inclusive bound): ceil(n/4) + 1 per axis
+    int bx = (nx + 3) / 4 + 1, by = (ny + 3) / 4 + 1, bz = (nz + 3) / 4 + 1;
+    int tx = (bx + 1) / 2, ty = (by + 1) / 2, tz = (bz + 1) / 2;
+    unsigned long long nbricks = (unsigned long long)bx * by * bz;
     unsigned long long ntiles = (unsigned long long)tx * ty * tz;
-    if (ntiles * 8ull >= (1ull << 32))
+    if (nbricks >= (1ull << 32))
         return fail(VXL_ERR_OUT_OF_RANGE, "grid_create: %dx%dx%d needs more than 2^32 brick words", nx, ny, nz);
     VXL_TRY(set_device(ctx));
     vxl_grid* g = new (std::nothrow) vxl_grid();
@@ -229,10 +270,13 @@ vxl_status vxl_grid_create(vxl_ctx* ctx, int nx, int ny, int nz, vxl_grid** out)
     g->nx = nx;
     g->ny = ny;
     g->nz = nz;
+    g->bx = bx;
+    g->by = by;
+    g->bz = bz;
     g->tx = tx;
     g->ty = ty;
     g->tz = tz;
-    g->nwords = (size_t)ntiles * 8;
+    g->nwords = (size_t)nbricks;
     g->nmask = (size_t)((ntiles + 31) / 32);
     cudaError_t e = cudaMalloc(&g->words, g->nwords * sizeof(uint64_t));
     if (e == cudaSuccess) e = cudaMalloc(&g->tmask, g->nmask * sizeof(uint32_t));
@@ -262,6 +306,9 @@ vxl_status vxl_grid_describe(const vxl_grid* g, vxl_grid_desc* out) {
     out->nx = g->nx;
     out->ny = g->ny;
     out->nz = g->nz;
+    out->bx = g->bx;
+    out->by = g->by;
+    out->bz = g->bz;
     out->tx = g->tx;
     out->ty = g->ty;
     out->tz = g->tz;

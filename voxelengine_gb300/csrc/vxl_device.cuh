@@ -15,21 +15,37 @@ namespace vxl {
 
 // ------------------------------------------------------------------ grid
 // Fine voxel (x,y,z) lives in the 4x4x4 brick word
-//   tile = (x>>3) + (y>>3)*tx + (z>>3)*tx*ty,  word = tile*8 + ((x>>2)&1) + ((y>>2)&1)*2 + ((z>>2)&1)*4
-// at bit (x&3) + (y&3)*4 + (z&3)*16. Each tile (8^3 voxels) is 64 bytes.
-// One zero tile pads the + side of every axis, so cells up to n+1 (the
-// reference DDA's inclusive upper bound) address valid, empty memory.
+//   word = (x>>2) + (y>>2)*bx + (z>>2)*bx*by       (bricks in x-fastest order)
+// at bit (x&3) + (y&3)*4 + (z&3)*16. One zero brick pads the + side of every
+// axis, so cells up to n+1 (the reference DDA's inclusive upper bound) address
+// valid, empty memory. A separate bitmap holds one bit per 8^3 tile
+// (tile (x>>3) + (y>>3)*tx + (z>>3)*tx*ty), set when any voxel of it is set.
 struct GridView {
     const uint64_t* __restrict__ words;
     const uint32_t* __restrict__ tmask;
     int nx, ny, nz;
-    int tx, ty, tz;
-    uint32_t txy;
+    int bx;        // bricks along x (padding included)
+    uint32_t bxy;  // bricks per z slice
+    int tx;        // tiles along x
+    uint32_t txy;  // tiles per z slice
 };
 
+inline GridView view_of(const vxl_grid* g) {
+    GridView v;
+    v.words = g->words;
+    v.tmask = g->tmask;
+    v.nx = g->nx;
+    v.ny = g->ny;
+    v.nz = g->nz;
+    v.bx = g->bx;
+    v.bxy = (uint32_t)g->bx * (uint32_t)g->by;
+    v.tx = g->tx;
+    v.txy = (uint32_t)g->tx * (uint32_t)g->ty;
+    return v;
+}
+
 __device__ __forceinline__ uint32_t word_index(const GridView& g, int x, int y, int z) {
-    uint32_t tile = (uint32_t)(x >> 3) + (uint32_t)(y >> 3) * (uint32_t)g.tx + (uint32_t)(z >> 3) * g.txy;
-    return tile * 8u + (uint32_t)(((x >> 2) & 1) | (((y >> 2) & 1) << 1) | (((z >> 2) & 1) << 2));
+    return (uint32_t)(x >> 2) + (uint32_t)(y >> 2) * (uint32_t)g.bx + (uint32_t)(z >> 2) * g.bxy;
 }
 __device__ __forceinline__ uint32_t bit_index(int x, int y, int z) {
     return (uint32_t)((x & 3) | ((y & 3) << 2) | ((z & 3) << 4));
@@ -230,61 +246,145 @@ static __device__ __noinline__ Hit dda_literal(const GridView& g, f3 o, f3 d, fl
 // reduce to sums of the selected components (unselected components are > 0,
 // so their products are +0). The 4^3 brick word of the current cell is kept
 // in a register and reloaded only when the cell leaves it.
-__device__ __forceinline__ Hit dda_fast(const GridView& g, f3 o, f3 d, float maxt) {
-    Hit r{0, 0, 0, 0.0f, 0, 0};
-    const int stx = d.x > 0.0f ? 1 : -1, sty = d.y > 0.0f ? 1 : -1, stz = d.z > 0.0f ? 1 : -1;
-    const float tdx = 1.0f / fabsf(d.x), tdy = 1.0f / fabsf(d.y), tdz = 1.0f / fabsf(d.z);
-    int cx = (int)floorf(o.x), cy = (int)floorf(o.y), cz = (int)floorf(o.z);
-    float tx = (((float)cx + (stx > 0 ? 1.0f : 0.0f)) - o.x) / d.x;
-    float ty = (((float)cy + (sty > 0 ? 1.0f : 0.0f)) - o.y) / d.y;
-    float tz = (((float)cz + (stz > 0 ? 1.0f : 0.0f)) - o.z) / d.z;
-    const unsigned ux = (unsigned)g.nx + 1u, uy = (unsigned)g.ny + 1u, uz = (unsigned)g.nz + 1u;
-    uint32_t wcur = 0xffffffffu;
-    uint64_t word = 0;
-    int n = 0;
-    int steps = 0;
-    float best = 0.0f, totalt = 0.0f;
-    bool bx, by, bz;
-    for (;;) {
-        float m = fminf(fminf(tx, ty), tz);
-        bx = tx == m;
-        by = ty == m;
-        bz = tz == m;
-        if ((unsigned)cx > ux || (unsigned)cy > uy || (unsigned)cz > uz) {
-            r.flags = VXL_RF_EXIT_BOUNDS;
-            best = totalt;
-            break;
+struct DState {
+    int cx, cy, cz;
+    float tx, ty, tz;
+    float tdx, tdy, tdz;
+    int sx, sy, sz;   // step signs, +1 / -1
+    float maxt;
+    float tot;        // totalt: best_t of the previous step
+    int n;            // the reference's n; also the number of fetches made
+    bool leap;        // empty bricks may be crossed in one go (see dda_leap)
+    uint32_t wcur;
+    uint64_t word;
+};
+
+// state after `vec3 stepSign = sign(direction) ... t_max = ...` (Light.frag:32-46)
+__device__ __forceinline__ void dda_init(DState& s, f3 o, f3 d, float maxt) {
+    s.sx = d.x > 0.0f ? 1 : -1;
+    s.sy = d.y > 0.0f ? 1 : -1;
+    s.sz = d.z > 0.0f ? 1 : -1;
+    s.tdx = 1.0f / fabsf(d.x);
+    s.tdy = 1.0f / fabsf(d.y);
+    s.tdz = 1.0f / fabsf(d.z);
+    s.cx = (int)floorf(o.x);
+    s.cy = (int)floorf(o.y);
+    s.cz = (int)floorf(o.z);
+    s.tx = (((float)s.cx + (s.sx > 0 ? 1.0f : 0.0f)) - o.x) / d.x;
+    s.ty = (((float)s.cy + (s.sy > 0 ? 1.0f : 0.0f)) - o.y) / d.y;
+    s.tz = (((float)s.cz + (s.sz > 0 ? 1.0f : 0.0f)) - o.z) / d.z;
+    s.maxt = maxt;
+    s.tot = 0.0f;
+    s.n = 0;
+    s.leap = false;
+    s.wcur = 0xffffffffu;
+    s.word = 0;
+}
+
+// Whether a ray may leap: the 256-iteration cap of Light.frag:75 can never be
+// reached before totalt >= maxt. Axis i crosses at most maxt*|d_i| + 2 cell
+// faces before time maxt, so with maxt*|d|_1 < 240 the loop always ends by
+// maxt, a hit or the bounds, and n no longer affects the result.
+__device__ __forceinline__ bool leap_allowed(f3 d, float maxt) {
+    return maxt * (fabsf(d.x) + fabsf(d.y) + fabsf(d.z)) < 240.0f;
+}
+
+// Cross the empty 4^3 brick holding the current cell in one go. Inside an
+// empty brick every test misses, so the iterations until the cell leaves the
+// brick only move the per-axis state: axis i crosses its faces at the times
+// T_i(0) = t_i, T_i(j+1) = T_i(j) + td_i (the same float adds the stepping
+// does), the brick is left at X = min_i T_i(e_i - 1) (e_i = cells to the brick
+// face), and every crossing at a time <= X is taken, ties included. Exact when
+// no iteration before the exit can stop the loop: totalt of an iteration is
+// at most 3*time, so fl(3X) < maxt suffices (the cap is excluded by
+// leap_allowed). totalt after the exit iteration is the sum of the t_max
+// components equal to X. Returns false (state untouched) if the condition fails.
+__device__ __forceinline__ bool dda_leap(DState& s) {
+    const int lx = s.cx & 3, ly = s.cy & 3, lz = s.cz & 3;
+    const int ex = s.sx > 0 ? 4 - lx : lx + 1;
+    const int ey = s.sy > 0 ? 4 - ly : ly + 1;
+    const int ez = s.sz > 0 ? 4 - lz : lz + 1;
+    float xx = s.tx, xy = s.ty, xz = s.tz;
+    for (int j = 1; j < ex; j++) xx = xx + s.tdx;
+    for (int j = 1; j < ey; j++) xy = xy + s.tdy;
+    for (int j = 1; j < ez; j++) xz = xz + s.tdz;
+    const float X = fminf(fminf(xx, xy), xz);
+    if (!(3.0f * X < s.maxt)) return false;
+    int kx = 0, ky = 0, kz = 0;
+    float px = s.tx, py = s.ty, pz = s.tz;  // last crossing time taken per axis
+    for (; kx < ex && s.tx <= X; kx++) { px = s.tx; s.tx = s.tx + s.tdx; }
+    for (; ky < ey && s.ty <= X; ky++) { py = s.ty; s.ty = s.ty + s.tdy; }
+    for (; kz < ez && s.tz <= X; kz++) { pz = s.tz; s.tz = s.tz + s.tdz; }
+    s.cx += s.sx * kx;
+    s.cy += s.sy * ky;
+    s.cz += s.sz * kz;
+    s.n += kx + ky + kz;
+    // the exit iteration selects the axes whose crossing time equals X
+    const bool ax = kx > 0 && px == X, ay = ky > 0 && py == X, az = kz > 0 && pz == X;
+    float best = (ax ? X : 0.0f) + (ay ? X : 0.0f);
+    s.tot = best + (az ? X : 0.0f);
+    return true;
+}
+
+// Up to `budget` iterations of the inner do-while of Light.frag:50-75.
+// Returns 0 while the ray goes on; otherwise the record flags, r filled in.
+// After a leap (s.leap) a miss may report an approximate cell, t and count;
+// hits are always found by exact stepping.
+template <bool LEAP = false>
+__device__ __forceinline__ int dda_run(const GridView& g, DState& s, Hit& r, int budget) {
+    for (int it = 0; it < budget; it++) {
+        if ((unsigned)s.cx > (unsigned)g.nx + 1u || (unsigned)s.cy > (unsigned)g.ny + 1u ||
+            (unsigned)s.cz > (unsigned)g.nz + 1u) {
+            r = Hit{s.cx, s.cy, s.cz, s.tot, s.n, VXL_RF_EXIT_BOUNDS};
+            return VXL_RF_EXIT_BOUNDS;
         }
-        steps++;
-        uint32_t wi = word_index(g, cx, cy, cz);
-        if (wi != wcur) {
-            wcur = wi;
-            word = __ldg(g.words + wi);
+        const uint32_t wi = word_index(g, s.cx, s.cy, s.cz);
+        if (wi != s.wcur) {
+            s.wcur = wi;
+            s.word = __ldg(g.words + wi);
         }
-        best = (bx ? tx : 0.0f) + (by ? ty : 0.0f);
-        best = best + (bz ? tz : 0.0f);
-        if ((word >> bit_index(cx, cy, cz)) & 1ull) {
-            r.flags = VXL_RF_HIT | (bx ? VXL_RF_SELX : 0) | (by ? VXL_RF_SELY : 0) | (bz ? VXL_RF_SELZ : 0);
-            break;
+        if (LEAP && s.leap && s.word == 0ull && dda_leap(s)) {
+            if (!(s.tot < s.maxt)) {
+                r = Hit{s.cx, s.cy, s.cz, s.tot, s.n, VXL_RF_EXIT_MAXT};
+                return VXL_RF_EXIT_MAXT;
+            }
+            continue;
         }
-        if (bx) { cx += stx; tx = tx + tdx; }
-        if (by) { cy += sty; ty = ty + tdy; }
-        if (bz) { cz += stz; tz = tz + tdz; }
-        totalt = best;
-        if (!(++n < 256 && totalt < maxt)) {
-            r.flags = n >= 256 ? VXL_RF_EXIT_STEPS : VXL_RF_EXIT_MAXT;
+        const float m = fminf(fminf(s.tx, s.ty), s.tz);
+        const bool bx = s.tx == m, by = s.ty == m, bz = s.tz == m;
+        // dot(t_max, select): the minimum itself unless several axes tie
+        // (+0.0f turns a -0 minimum into the +0 the dot product gives)
+        float best = m + 0.0f;
+        if ((bx && (by || bz)) || (by && bz)) {
+            best = (bx ? s.tx : 0.0f) + (by ? s.ty : 0.0f);
+            best = best + (bz ? s.tz : 0.0f);
+        }
+        if ((s.word >> bit_index(s.cx, s.cy, s.cz)) & 1ull) {
+            const int f = VXL_RF_HIT | (bx ? VXL_RF_SELX : 0) | (by ? VXL_RF_SELY : 0) | (bz ? VXL_RF_SELZ : 0);
+            r = Hit{s.cx, s.cy, s.cz, best, s.n + 1, f};
+            return f;
+        }
+        const int px = s.cx, py = s.cy, pz = s.cz;
+        if (bx) { s.cx += s.sx; s.tx = s.tx + s.tdx; }
+        if (by) { s.cy += s.sy; s.ty = s.ty + s.tdy; }
+        if (bz) { s.cz += s.sz; s.tz = s.tz + s.tdz; }
+        s.tot = best;
+        if (!(++s.n < 256 && best < s.maxt)) {
             // the record reports the last cell tested, not the advanced one
-            if (bx) cx -= stx;
-            if (by) cy -= sty;
-            if (bz) cz -= stz;
-            break;
+            const int f = s.n >= 256 ? VXL_RF_EXIT_STEPS : VXL_RF_EXIT_MAXT;
+            r = Hit{px, py, pz, best, s.n, f};
+            return f;
         }
     }
-    r.vx = cx;
-    r.vy = cy;
-    r.vz = cz;
-    r.t = best;
-    r.steps = steps;
+    return 0;
+}
+
+__device__ __forceinline__ Hit dda_fast(const GridView& g, f3 o, f3 d, float maxt) {
+    DState s;
+    dda_init(s, o, d, maxt);
+    Hit r;
+    while (dda_run(g, s, r, 1 << 20) == 0) {
+    }
     return r;
 }
 

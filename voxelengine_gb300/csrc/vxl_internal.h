@@ -17,16 +17,24 @@ struct vxl_ctx {
     size_t d_scratch_bytes;
     void* d_stage;
     size_t d_stage_bytes;
+    // ring of work-queue counters for the persistent kernels: each launch
+    // takes the next one, so launches in flight on different streams never
+    // share a counter
+    int* d_counters;
+    uint32_t counter_next;
+    vxl_tuning tune;  // occlusion kernel launch shape (vxl_ctx_set_tuning)
 };
+constexpr uint32_t kCounterRing = 4096;
 
 struct vxl_grid {
     vxl_ctx* ctx;
     int nx, ny, nz;
-    int tx, ty, tz;
+    int bx, by, bz;  // 4^3 bricks per axis, one padding brick included
+    int tx, ty, tz;  // 8^3 tiles per axis (tile map)
     uint64_t* words;
     size_t nwords;
     uint32_t* tmask;
-    size_t nmask;  // uint32 words of the tile mask
+    size_t nmask;  // uint32 words of the tile map
 };
 
 namespace vxl {
@@ -76,6 +84,11 @@ vxl_status launch_trace_rays(vxl_ctx* ctx, const vxl_grid* g, const float* rays,
                              vxl_ray_record* rec, cudaStream_t s);
 vxl_status launch_trace_occlusion(vxl_ctx* ctx, const vxl_grid* g, const vxl_gbuffer* gb, const vxl_trace_params* p,
                                   const vxl_outputs* out, cudaStream_t s);
+bool occl_pool_supported(const vxl_grid* g, const vxl_trace_params* p);
+vxl_status launch_trace_occlusion_pool(vxl_ctx* ctx, const vxl_grid* g, const vxl_gbuffer* gb,
+                                       const vxl_trace_params* p, const vxl_outputs* out, int* d_counter,
+                                       const vxl_tuning& tune, cudaStream_t s);
+int* ctx_next_counter(vxl_ctx* ctx);
 vxl_status launch_light_ambient(vxl_ctx* ctx, const vxl_grid* g, const float* wcp, const float* nrm,
                                 const float* depth, const float* noise, int64_t npix, float* shadow, float* irr,
                                 vxl_ray_record* rec, cudaStream_t s);
