@@ -75,10 +75,10 @@ __device__ __forceinline__ f3 gen_dir(const TraceConstsP& c, int k, uint32_t pix
     return normalize(sub(mul(H, 2.0f * vh), V));
 }
 
-template <int TP, int KSTEP, bool LEAP, bool RECORDS>
 #ifndef VXL_POOL_MIN_BLOCKS
 #define VXL_POOL_MIN_BLOCKS 8  // 8 blocks of 4 warps: 64 registers per thread
 #endif
+template <int TP, int KSTEP, bool LEAP, bool RECORDS>
 __global__ void __launch_bounds__(128, VXL_POOL_MIN_BLOCKS) k_occl_pool(GridView g, const float* __restrict__ pos,
                                                    const float* __restrict__ nrm, const float* __restrict__ rough,
                                                    int64_t npix, TraceConstsP c, float* __restrict__ o_shadow,
