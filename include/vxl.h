@@ -264,6 +264,32 @@ vxl_status vxl_shadowvox_update(vxl_ctx* ctx, vxl_grid* grid, const vxl_model* m
 vxl_status vxl_vox_destroyed(vxl_ctx* ctx, vxl_grid* grid, const vxl_model* model, const float world[16],
                              int32_t* h_region, void* stream);
 
+/* vxl_voxelize for callers that cannot allocate device memory: an engine or
+ * render loop that commits its device memory up front, code that runs on a
+ * pool-managed budget, or updates issued between frames where a cudaMalloc
+ * would stall the GPU. This entry point has no counterpart in the reference
+ * (whose voxelizer runs on the CPU); it exists for such callers only.
+ *  - It allocates nothing: no context, no grid handle, no cudaMalloc/cudaFree
+ *    and no heap allocation. The caller passes the grid descriptor (device
+ *    words and tile map in the vxl_grid_desc layout, e.g. from
+ *    vxl_grid_describe), the models and instances (host arrays, as for
+ *    vxl_voxelize) and the optional device aabb output.
+ *  - Its scratch is a fixed table in the library's static device memory
+ *    (about 1.2 MiB, held on every GPU that loads libvxl until the process
+ *    exits): at most VXL_NOALLOC_MAX_INSTANCES instances and
+ *    VXL_NOALLOC_MAX_MODELS models per call; larger calls are rejected with
+ *    VXL_ERR_OUT_OF_RANGE.
+ *  - The first call on a device looks up the table's device address (once per
+ *    device, with that device current); make that first call before any stream
+ *    capture.
+ *  - All calls share the one table: calls that overlap on the GPU (other
+ *    streams, other host threads) race and must be serialised by the caller.
+ *  - Same result as vxl_voxelize; returns when the update is complete. */
+#define VXL_NOALLOC_MAX_INSTANCES 16384
+#define VXL_NOALLOC_MAX_MODELS 4096
+vxl_status vxl_voxelize_noalloc(const vxl_grid_desc* grid, const vxl_model* models, int nmodels,
+                                const vxl_instance* instances, int n, int32_t* d_aabb, void* stream);
+
 /* .v asset reader (VoxAsset::Serialize, VoxAsset.h:42-50): u32 sx,sy,sz then
  * sx*sy*sz bytes. Query with data == NULL to get the sizes, then read into a
  * host buffer of sx*sy*sz bytes. */

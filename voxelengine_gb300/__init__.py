@@ -35,7 +35,8 @@ EXPORTED = [
     "vxl_ctx_launch_count", "vxl_ctx_set_tuning", "vxl_ctx_get_tuning", "vxl_grid_create", "vxl_grid_destroy", "vxl_grid_describe", "vxl_grid_clear",
     "vxl_grid_build_bricks", "vxl_grid_import_r8", "vxl_grid_export_r8", "vxl_grid_import_palette",
     "vxl_grid_count", "vxl_trace_rays", "vxl_trace_occlusion", "vxl_trace_occlusion_host", "vxl_light_ambient",
-    "vxl_light_reflection", "vxl_light_point", "vxl_voxelize", "vxl_shadowvox_update", "vxl_vox_destroyed",
+    "vxl_light_reflection", "vxl_light_point", "vxl_voxelize", "vxl_voxelize_noalloc", "vxl_shadowvox_update",
+    "vxl_vox_destroyed",
     "vxl_read_v", "vxl_scene_noise", "vxl_scene_boxes", "vxl_scene_gbuffer",
 ]
 
@@ -134,6 +135,8 @@ def lib():
         L.vxl_light_reflection.argtypes = [vp, vp, vp, vp, vp, vp, vp, i64, vp, vp, vp]
         L.vxl_light_point.argtypes = [vp, vp, vp, vp, vp, i64, C.POINTER(f * 3), f, C.c_int, vp, vp, vp]
         L.vxl_voxelize.argtypes = [vp, vp, C.POINTER(Model), C.c_int, C.POINTER(Instance), C.c_int, vp, vp]
+        L.vxl_voxelize_noalloc.argtypes = [C.POINTER(GridDesc), C.POINTER(Model), C.c_int, C.POINTER(Instance),
+                                           C.c_int, vp, vp]
         L.vxl_shadowvox_update.argtypes = [vp, vp, C.POINTER(Model), C.c_int, C.POINTER(Entity), C.c_int, vp, vp]
         L.vxl_vox_destroyed.argtypes = [vp, vp, C.POINTER(Model), C.POINTER(f * 16), vp, vp]
         L.vxl_read_v.argtypes = [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), vp,
@@ -343,6 +346,19 @@ def voxelize(ctx, grid, models, instances, d_aabb=None, stream=None):
         arr[i].model, arr[i].op = mi, op
     check(lib().vxl_voxelize(ctx.handle, grid.handle, ms, len(models), arr, len(instances), _ptr(d_aabb),
                              _stream(stream)))
+
+
+def voxelize_noalloc(grid_desc, models, instances, d_aabb=None, stream=None):
+    """vxl_voxelize_noalloc: like voxelize(), for callers that cannot allocate:
+    takes a GridDesc (no context, no grid handle) and uses the library's fixed
+    static device table as its only scratch."""
+    ms = _models(models)
+    arr = (Instance * max(1, len(instances)))()
+    for i, (m, mi, op) in enumerate(instances):
+        arr[i].matrix[:] = [float(x) for x in np.asarray(m, np.float32).reshape(16)]
+        arr[i].model, arr[i].op = mi, op
+    check(lib().vxl_voxelize_noalloc(C.byref(grid_desc), ms, len(models), arr, len(instances), _ptr(d_aabb),
+                                     _stream(stream)))
 
 
 def shadowvox_update(ctx, grid, models, entities, stream=None):

@@ -304,6 +304,14 @@ vxl_status launch_build_tile_mask(vxl_grid* g, cudaStream_t s) {
     return VXL_OK;
 }
 
+cudaError_t launch_tile_mask_view(const GridView& v, uint32_t* mask, int by, int bz, int tx, int ty, int tz,
+                                  cudaStream_t s) {
+    uint32_t ntiles = (uint32_t)((size_t)tx * ty * tz);
+    uint32_t nmask = (ntiles + 31) / 32;
+    k_tile_mask<<<blocks_for((size_t)nmask * 32, 256), 256, 0, s>>>(v, mask, by, bz, ntiles, nmask);
+    return cudaGetLastError();
+}
+
 vxl_status launch_grid_count(const vxl_grid* g, unsigned long long* d_out, cudaStream_t s) {
     k_count<<<g->ctx->sm_count * 4, 256, 0, s>>>(g->words, g->nwords, d_out);
     g->ctx->launches++;
