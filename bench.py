@@ -53,6 +53,18 @@ def light_dir(seed):
     return (v / np.linalg.norm(v)).astype(np.float32)
 
 
+def profiled_traffic(workload):
+    """DRAM bytes per launch of the occlusion kernel from the committed ncu
+    summary of this workload (profiles/k_occl_pool_<workload>.md), or None."""
+    p = os.path.join(ROOT, "profiles", "k_occl_pool_%s.md" % workload)
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch:"):
+            return int(line.split(":")[1])
+    return None
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -84,7 +96,7 @@ class ClockSampler:
                     self.rows.append([c.strip() for c in out.stdout.strip().split(",")])
             except Exception:
                 pass
-            self._stop.wait(0.2)
+            self._stop.wait(0.02)
 
     def __enter__(self):
         self._t = threading.Thread(target=self._run, daemon=True)
@@ -189,9 +201,10 @@ def run_reference(args, wl):
                            ao_len=wl["ao_len"], spec_len=wl["spec_len"], n_shadow=wl["n_shadow"], n_ao=wl["n_ao"],
                            n_spec=wl["n_spec"], seed=wl["seed"])
     per_step = []
+    # each step is a bounded sample; the whole run stays within ~150 s of CPU work
+    budget = min(args.ref_step_seconds, 150.0 / max(1, args.warmup + args.steps))
     for s in range(args.warmup + args.steps):
-        v, rows, dt, th = cpu_sample_rays_per_s(g, pos, nrm, rough, P, W, H, budget_s=args.ref_step_seconds,
-                                                threads=threads)
+        v, rows, dt, th = cpu_sample_rays_per_s(g, pos, nrm, rough, P, W, H, budget_s=budget, threads=threads)
         if s >= args.warmup:
             per_step.append((v, rows, dt))
     rays_s = sum(v * dt for v, _, dt in per_step) / sum(dt for _, _, dt in per_step)
@@ -206,7 +219,7 @@ def run_reference(args, wl):
         "cpu_baseline": {"value": val, "unit": "Grays/s", "cores": threads, "kind": "port",
                          "sample": "per step: whole image rows in seeded random order until %.0f s of wall time "
                                    "(%d rows of %d on average), %d rays per pixel" % (
-                                       args.ref_step_seconds, statistics.mean(r for _, r, _ in per_step), H, R)},
+                                       budget, statistics.mean(r for _, r, _ in per_step), H, R)},
         "e2e": {"value": val, "unit": "Grays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -263,12 +276,15 @@ def run_gpu(args, wl):
 
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
-    for _ in range(args.warmup):
-        V.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, **outs)
-    torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    l0 = ctx.launch_count()
+    # clocks are sampled from the start of the warm-up (same load) to the end
+    # of the timed steps: the timed region alone is often shorter than one
+    # nvidia-smi query
     with ClockSampler(local) as clk:
+        for _ in range(args.warmup):
+            V.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, **outs)
+        torch.cuda.synchronize()
+        l0 = ctx.launch_count()
         barrier(dist)
         torch.cuda.synchronize()
         for s in range(args.steps):
@@ -321,7 +337,9 @@ def run_gpu(args, wl):
         "rays_per_step": rays_per_step, "valid_pixels": valid, "s_ref_mean_fetches_per_ray": s_ref,
         "hit_fraction": hits,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "peak_kind": peak_kind,
+                     "traffic": profiled_traffic(args.workload), "peak_kind": peak_kind,
+                     "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one launch, "
+                                       "profiles/k_occl_pool_%s.md" % args.workload,
                      "bytes_per_ray": b_ray,
                      "note": "algorithmic bytes = ((28 B in + 20 B out) per pixel)/R + 4 B x S_ref per ray; "
                              "per-launch time from CUDA events on the launch stream"},
@@ -352,8 +370,8 @@ def run_gpu(args, wl):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="vxl", choices=["vxl", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
