@@ -62,6 +62,9 @@ typedef struct vxl_tuning {
     int32_t kstep;     /* DDA iterations between pool refills: 1, 2, 4 or 8 */
     int32_t leap;      /* 1: cross empty bricks in one step where exact; 2: never */
     int32_t order;     /* 1: dispatch spec, shadow, AO; 2: shadow, AO, spec */
+    int32_t tile_w;    /* tile shape: pixels per tile row (tile_px = runs of pixels; 4 or 8 = image blocks,
+                          used when the G-buffer's width * height == npix) */
+    int32_t grab;      /* tiles a warp takes per work-queue access: 1, 2 or 4 */
 } vxl_tuning;
 vxl_status vxl_ctx_set_tuning(vxl_ctx* ctx, const vxl_tuning* t);
 vxl_status vxl_ctx_get_tuning(const vxl_ctx* ctx, vxl_tuning* out);
@@ -193,6 +196,29 @@ vxl_status vxl_trace_occlusion_host(vxl_ctx* ctx, const vxl_grid* grid, const fl
                                     const float* h_rough, int64_t npix, const vxl_trace_params* params,
                                     float* h_shadow, float* h_ao, float* h_ao_vis, float* h_spec, float* h_spec_t,
                                     void* stream);
+
+/* ------------------------------------------------------------ batched form
+ * Many scenes (grids of any size, G-buffers of any size) traced by ONE
+ * persistent launch: all scenes' pixel tiles share one work queue, so large
+ * and small scenes keep every SM busy (no reference counterpart: the engine
+ * traces one view per frame). The plan uploads the scene table once and
+ * captures the launch (queue reset + kernel) in a CUDA graph; each run
+ * replays the graph. The items' buffers must stay valid while the batch
+ * exists. Runs of the same batch must not overlap (they share one queue). */
+typedef struct vxl_batch vxl_batch;
+typedef struct vxl_batch_item {
+    const vxl_grid* grid;
+    vxl_gbuffer gbuf;
+    vxl_trace_params params;
+    vxl_outputs out;        /* records must be NULL in a batch */
+} vxl_batch_item;
+
+/* use_graph: 1 = capture the launch in a CUDA graph (run replays it), 0 = launch directly */
+vxl_status vxl_batch_create(vxl_ctx* ctx, const vxl_batch_item* items, int n, int use_graph, vxl_batch** out);
+vxl_status vxl_batch_run(vxl_batch* batch, void* stream);
+vxl_status vxl_batch_destroy(vxl_batch* batch);
+/* total pixel tiles and traced-ray upper bound (pixels x rays per pixel) of a batch */
+vxl_status vxl_batch_info(const vxl_batch* batch, int64_t* tiles, int64_t* rays);
 
 /* ------------------------------------------------ reference light passes
  * Bit-exact replacements for the live shader passes (Sparse/SuperSparse

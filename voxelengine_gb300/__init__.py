@@ -34,7 +34,8 @@ EXPORTED = [
     "vxl_abi_version", "vxl_last_error_string", "vxl_status_string", "vxl_ctx_create", "vxl_ctx_destroy",
     "vxl_ctx_launch_count", "vxl_ctx_set_tuning", "vxl_ctx_get_tuning", "vxl_grid_create", "vxl_grid_destroy", "vxl_grid_describe", "vxl_grid_clear",
     "vxl_grid_build_bricks", "vxl_grid_import_r8", "vxl_grid_export_r8", "vxl_grid_import_palette",
-    "vxl_grid_count", "vxl_trace_rays", "vxl_trace_occlusion", "vxl_trace_occlusion_host", "vxl_light_ambient",
+    "vxl_grid_count", "vxl_trace_rays", "vxl_trace_occlusion", "vxl_trace_occlusion_host", "vxl_batch_create",
+    "vxl_batch_run", "vxl_batch_destroy", "vxl_batch_info", "vxl_light_ambient",
     "vxl_light_reflection", "vxl_light_point", "vxl_voxelize", "vxl_voxelize_noalloc", "vxl_shadowvox_update",
     "vxl_vox_destroyed",
     "vxl_read_v", "vxl_scene_noise", "vxl_scene_boxes", "vxl_scene_gbuffer",
@@ -71,10 +72,15 @@ class Outputs(C.Structure):
 
 
 class Tuning(C.Structure):
-    _fields_ = [("tile_px", C.c_int32), ("kstep", C.c_int32), ("leap", C.c_int32), ("order", C.c_int32)]
+    _fields_ = [("tile_px", C.c_int32), ("kstep", C.c_int32), ("leap", C.c_int32), ("order", C.c_int32),
+                ("tile_w", C.c_int32), ("grab", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class BatchItem(C.Structure):
+    _fields_ = [("grid", C.c_void_p), ("gbuf", GBuffer), ("params", TraceParams), ("out", Outputs)]
 
 
 class Model(C.Structure):
@@ -131,6 +137,10 @@ def lib():
         L.vxl_trace_rays.argtypes = [vp, vp, vp, i64, C.c_int, vp, vp]
         L.vxl_trace_occlusion.argtypes = [vp, vp, C.POINTER(GBuffer), C.POINTER(TraceParams), C.POINTER(Outputs), vp]
         L.vxl_trace_occlusion_host.argtypes = [vp, vp, vp, vp, vp, i64, C.POINTER(TraceParams), vp, vp, vp, vp, vp, vp]
+        L.vxl_batch_create.argtypes = [vp, C.POINTER(BatchItem), C.c_int, C.c_int, C.POINTER(vp)]
+        L.vxl_batch_run.argtypes = [vp, vp]
+        L.vxl_batch_destroy.argtypes = [vp]
+        L.vxl_batch_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         L.vxl_light_ambient.argtypes = [vp, vp, vp, vp, vp, vp, i64, vp, vp, vp, vp]
         L.vxl_light_reflection.argtypes = [vp, vp, vp, vp, vp, vp, vp, i64, vp, vp, vp]
         L.vxl_light_point.argtypes = [vp, vp, vp, vp, vp, i64, C.POINTER(f * 3), f, C.c_int, vp, vp, vp]
@@ -200,8 +210,8 @@ class Context:
         check(lib().vxl_ctx_launch_count(self._h, C.byref(n)))
         return n.value
 
-    def set_tuning(self, tile_px=0, kstep=0, leap=0, order=0):
-        t = Tuning(tile_px, kstep, leap, order)
+    def set_tuning(self, tile_px=0, kstep=0, leap=0, order=0, tile_w=0, grab=0):
+        t = Tuning(tile_px, kstep, leap, order, tile_w, grab)
         check(lib().vxl_ctx_set_tuning(self._h, C.byref(t)))
 
     def get_tuning(self) -> dict:
@@ -306,6 +316,47 @@ def trace_occlusion_host(ctx: Context, grid: Grid, h_pos, h_nrm, h_rough, npix: 
     check(lib().vxl_trace_occlusion_host(ctx.handle, grid.handle, _ptr(h_pos), _ptr(h_nrm), _ptr(h_rough), npix,
                                          C.byref(params), _ptr(h_shadow), _ptr(h_ao), _ptr(h_ao_vis), _ptr(h_spec),
                                          _ptr(h_spec_t), _stream(stream)))
+
+
+class Batch:
+    """vxl_batch: many scenes traced by one persistent launch (CUDA-graph replay).
+
+    items: list of dicts with keys grid, pos, nrm, rough, npix, width, height,
+    params, and output tensors shadow/ao/ao_vis/spec/spec_t (any may be None).
+    The tensors must stay alive while the batch exists (kept referenced here)."""
+
+    def __init__(self, ctx: Context, items, use_graph=True):
+        self.ctx = ctx
+        self._keep = items
+        arr = (BatchItem * len(items))()
+        for i, it in enumerate(items):
+            arr[i].grid = it["grid"].handle.value
+            arr[i].gbuf = GBuffer(_ptr(it["pos"]), _ptr(it["nrm"]), _ptr(it.get("rough")), it["npix"],
+                                  it.get("width", 0), it.get("height", 0))
+            arr[i].params = it["params"]
+            arr[i].out = Outputs(_ptr(it.get("shadow")), _ptr(it.get("ao")), _ptr(it.get("ao_vis")),
+                                 _ptr(it.get("spec")), _ptr(it.get("spec_t")), None)
+        self._h = C.c_void_p()
+        check(lib().vxl_batch_create(ctx.handle, arr, len(items), 1 if use_graph else 0, C.byref(self._h)))
+
+    def run(self, stream=None):
+        check(lib().vxl_batch_run(self._h, _stream(stream)))
+
+    def info(self):
+        t, r = C.c_int64(), C.c_int64()
+        check(lib().vxl_batch_info(self._h, C.byref(t), C.byref(r)))
+        return t.value, r.value
+
+    def close(self):
+        if self._h:
+            lib().vxl_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def light_ambient(ctx, grid, wcp, nrm, depth, noise, npix, shadow, irradiance, records=None, stream=None):

@@ -1,18 +1,21 @@
-// occlusion.cu — DDA-mode occlusion pass (vxl_trace_occlusion), persistent
-// and warp-pooled.
+// occlusion.cu — DDA-mode occlusion pass (vxl_trace_occlusion) and its
+// batched form (vxl_batch_*): persistent, warp-pooled.
 //
-// Each warp repeatedly takes a tile of TP pixels from a global tile counter:
+// Each warp repeatedly takes `grab` tiles of TP pixels from a global counter
+// (one counter for a whole batch of scenes: work stealing across scenes):
 //  A. Generation: the warp's lanes build every ray of the tile (shadow, AO,
 //     spec; same generator and arithmetic as the per-pixel reference kernel)
 //     and store each ray's DDA start state (cell, t_max, t_delta, signs) as a
 //     32-byte slot in shared memory, compacted so live rays are contiguous.
-//     This part has no divergence: all lanes run the same generator code.
+//     All lanes run the same generator code.
 //  B. Traversal: each lane takes the next slot whenever its ray ends, so the
 //     warp stays full while the pool lasts (rays end after very different
-//     numbers of steps). A lane runs up to KSTEP DDA steps between refills.
+//     numbers of steps). A lane runs up to KSTEP DDA iterations between refills.
 //  C. Reduction: one lane per pixel folds the ray results in the fixed order
 //     shadow, AO 0..n-1, spec 0..n-1, so outputs are bit-identical to the
 //     sequential per-pixel evaluation.
+// A tile is either a run of TP consecutive pixels or, when the image width is
+// known, a tile_w x (TP / tile_w) block of the image.
 #include "vxl_device.cuh"
 
 namespace vxl {
@@ -26,6 +29,27 @@ struct TraceConstsP {
     uint32_t seed_h;
 };
 
+// One scene of a launch: grid, G-buffer, outputs, tiling, ray parameters.
+struct SceneDesc {
+    GridView g;
+    const float* pos;
+    const float* nrm;
+    const float* rough;
+    float* o_shadow;
+    float* o_ao;
+    float* o_vis;
+    float* o_spec;
+    float* o_spec_t;
+    vxl_ray_record* rec;
+    int64_t npix;
+    int64_t tile_begin;  // first global tile of this scene (batched launches)
+    int64_t ntiles;
+    int width, height;   // image size, for block tiles
+    int tile_w;          // pixels per tile row; TP = runs of TP pixels
+    int pad;
+    TraceConstsP c;
+};
+
 struct __align__(16) PSlot {
     int c01;     // cx (low 16 bits, signed) | cy << 16
     int c2m;     // cz (low 16 bits, signed) | meta << 16
@@ -36,6 +60,7 @@ struct __align__(16) PSlot {
 // bit 14 empty bricks may be leapt (leap_allowed and no per-ray records requested)
 constexpr int kMetaLit = 1 << 3;
 constexpr int kMetaLeap = 1 << 14;
+constexpr int kPoolMaxR = 31;
 
 // shared memory of one warp's pool: slots, result t per ray, hit mask per ray index
 __host__ __device__ __forceinline__ size_t pool_bytes(int TP, int R) {
@@ -75,254 +100,270 @@ __device__ __forceinline__ f3 gen_dir(const TraceConstsP& c, int k, uint32_t pix
     return normalize(sub(mul(H, 2.0f * vh), V));
 }
 
+// pixel index of position p of a scene-local tile; false outside the image
+template <int TP>
+__device__ __forceinline__ bool tile_pixel(const SceneDesc& S, int64_t tile, int p, int64_t* gpix) {
+    if (S.tile_w >= TP || S.width <= 0) {
+        *gpix = tile * TP + p;
+        return *gpix < S.npix;
+    }
+    const int tw = S.tile_w, th = TP / tw;
+    const int64_t tpr = (S.width + tw - 1) / tw;
+    const int64_t ty = tile / tpr, tx = tile - ty * tpr;
+    const int64_t x = tx * tw + p % tw, y = ty * th + p / tw;
+    *gpix = y * S.width + x;
+    return x < S.width && y < S.height;
+}
+
+// Phases A-C for one tile of one scene.
+template <int TP, int KSTEP, bool LEAP, bool RECORDS>
+__device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView& g, int64_t tile, PSlot* slots,
+                                             float* res_t, uint32_t* res_hit, int lane) {
+    constexpr int LPP = 32 / TP;  // lanes per pixel during generation
+    const TraceConstsP& c = S.c;
+    const int R = c.R;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const unsigned ux = (unsigned)g.nx + 1u, uy = (unsigned)g.ny + 1u, uz = (unsigned)g.nz + 1u;
+
+    // ---------------------------------------------------------- A
+    const int p = lane % TP;
+    int64_t gpix;
+    const bool inimg = tile_pixel<TP>(S, tile, p, &gpix);
+    f3 P = mk(0.0f, 0.0f, 0.0f), N = mk(0.0f, 0.0f, 0.0f);
+    float ro = c.default_rough;
+    if (inimg) {
+        P = ld3(S.pos + 3 * gpix);
+        N = ld3(S.nrm + 3 * gpix);
+        if (S.rough) ro = S.rough[gpix];
+    }
+    const bool sky = !inimg || (N.x == 0.0f && N.y == 0.0f && N.z == 0.0f);
+    const f3 O = add(P, mul(N, c.bias));
+    f3 T, B;
+    tangent_frame(N, &T, &B);
+    for (int k = lane; k < R; k += 32) res_hit[k] = 0u;
+    int live = 0;
+    const int rounds = (R + LPP - 1) / LPP;
+    for (int j = 0; j < rounds; j++) {
+        // generation (= dispatch) order: spec rays first, then shadow, then
+        // AO, so the longest rays start early and the pool drains on short ones
+        const int kk = j * LPP + lane / TP;
+        const int k = !c.spec_first ? kk : (kk < c.n_spec ? c.n_shadow + c.n_ao + kk : kk - c.n_spec);
+        bool is_live = false;
+        PSlot sl;
+        if (kk < R && !sky) {
+            const f3 d = gen_dir(c, k, (uint32_t)gpix, P, N, T, B, ro);
+            const float maxt = kind_maxt(c, k);
+            int meta = (p << 4) | (k << 9);
+            Hit h0{0, 0, 0, 0.0f, 0, VXL_RF_EXIT_BOUNDS};
+            bool born_done = false;
+            if (!ray_domain_ok(O, d)) {
+                born_done = true;
+            } else if (!dir_fast_ok(d)) {
+                is_live = true;
+                sl.c01 = 0;
+                sl.c2m = (meta | kMetaLit) << 16;
+                sl.a0 = O.x; sl.a1 = O.y; sl.a2 = O.z;
+                sl.b0 = d.x; sl.b1 = d.y; sl.b2 = d.z;
+            } else {
+                DState s;
+                dda_init(s, O, d, maxt);
+                if ((unsigned)s.cx > ux || (unsigned)s.cy > uy || (unsigned)s.cz > uz) {
+                    born_done = true;  // origin cell out of bounds: the first test exits (Light.frag:53)
+                    h0 = Hit{s.cx, s.cy, s.cz, 0.0f, 0, VXL_RF_EXIT_BOUNDS};
+                } else {
+                    is_live = true;
+                    meta |= (s.sx < 0 ? 1 : 0) | (s.sy < 0 ? 2 : 0) | (s.sz < 0 ? 4 : 0);
+                    if (LEAP && !RECORDS && leap_allowed(d, maxt)) meta |= kMetaLeap;
+                    sl.c01 = (s.cx & 0xffff) | (s.cy << 16);
+                    sl.c2m = (s.cz & 0xffff) | (meta << 16);
+                    sl.a0 = s.tx; sl.a1 = s.ty; sl.a2 = s.tz;
+                    sl.b0 = s.tdx; sl.b1 = s.tdy; sl.b2 = s.tdz;
+                }
+            }
+            if (born_done) {
+                res_t[k * TP + p] = h0.t;
+                if (RECORDS) store_record(S.rec + gpix * R + k, h0);
+            }
+        } else if (kk < R && RECORDS && inimg) {
+            Hit z{0, 0, 0, 0.0f, 0, 0};
+            store_record(S.rec + gpix * R + k, z);
+        }
+        const unsigned lv = __ballot_sync(0xffffffffu, is_live);
+        if (is_live) slots[live + __popc(lv & lt_mask)] = sl;
+        live += __popc(lv);
+    }
+    __syncwarp();
+
+    // ---------------------------------------------------------- B
+    int base = 0;
+    int my = -1;
+    bool retired = false;
+    DState s;
+    int meta = 0;
+    for (;;) {
+        const bool need = my < 0 && !retired;
+        const unsigned nm = __ballot_sync(0xffffffffu, need);
+        if (nm) {
+            if (need) {
+                const int at = base + __popc(nm & lt_mask);
+                if (at < live) {
+                    const PSlot sl = slots[at];
+                    meta = (unsigned)sl.c2m >> 16;
+                    const int k = (meta >> 9) & 31;
+                    const float maxt = kind_maxt(c, k);
+                    if (meta & kMetaLit) {
+                        const Hit h = dda_literal(g, mk(sl.a0, sl.a1, sl.a2), mk(sl.b0, sl.b1, sl.b2), maxt);
+                        const int pp = (meta >> 4) & 31;
+                        res_t[k * TP + pp] = h.t;
+                        if (h.flags & VXL_RF_HIT) atomicOr(&res_hit[k], 1u << pp);
+                        if (RECORDS) {
+                            int64_t gp;
+                            tile_pixel<TP>(S, tile, pp, &gp);
+                            store_record(S.rec + gp * R + k, h);
+                        }
+                    } else {
+                        my = at;
+                        s.cx = lo16(sl.c01);
+                        s.cy = hi16(sl.c01);
+                        s.cz = lo16(sl.c2m);
+                        s.tx = sl.a0; s.ty = sl.a1; s.tz = sl.a2;
+                        s.tdx = sl.b0; s.tdy = sl.b1; s.tdz = sl.b2;
+                        s.sx = (meta & 1) ? -1 : 1;
+                        s.sy = (meta & 2) ? -1 : 1;
+                        s.sz = (meta & 4) ? -1 : 1;
+                        s.maxt = maxt;
+                        s.tot = 0.0f;
+                        s.n = 0;
+                        s.leap = (meta & kMetaLeap) != 0;
+                        s.wcur = 0xffffffffu;
+                        s.word = 0;
+                    }
+                } else {
+                    retired = true;
+                }
+            }
+            base += __popc(nm);
+        }
+        if (!__any_sync(0xffffffffu, my >= 0) && base >= live) break;
+        if (my >= 0) {
+            Hit h;
+            const int f = dda_run<LEAP>(g, s, h, KSTEP);
+            if (f) {
+                const int k = (meta >> 9) & 31, pp = (meta >> 4) & 31;
+                res_t[k * TP + pp] = h.t;
+                if (f & VXL_RF_HIT) atomicOr(&res_hit[k], 1u << pp);
+                if (RECORDS) {
+                    int64_t gp;
+                    tile_pixel<TP>(S, tile, pp, &gp);
+                    store_record(S.rec + gp * R + k, h);
+                }
+                my = -1;
+            }
+        }
+    }
+    __syncwarp();
+
+    // ---------------------------------------------------------- C
+    if (lane < TP && inimg) {
+        float sh = 1.0f, ao = 1.0f, vis = 1.0f, sp = 1.0f, st = c.spec_len;
+        if (!sky) {
+            int k = 0;
+            if (c.n_shadow > 0) {
+                sh = ((res_hit[0] >> p) & 1u) ? 0.0f : 1.0f;
+                k = 1;
+            }
+            float acc = 0.0f, v = 0.0f;
+            for (int j = 0; j < c.n_ao; j++, k++) {
+                const bool hit = (res_hit[k] >> p) & 1u;
+                const float t = res_t[k * TP + p];
+                float tt = hit ? (t < c.ao_len ? t : c.ao_len) : c.ao_len;
+                float q = tt / c.ao_len;
+                acc += q * q;
+                v += hit ? 0.0f : 1.0f;
+            }
+            if (c.n_ao > 0) {
+                ao = acc / (float)c.n_ao;
+                vis = v / (float)c.n_ao;
+            }
+            if (c.n_spec > 0) {
+                float spa = 0.0f, sta = 0.0f;
+                for (int j = 0; j < c.n_spec; j++, k++) {
+                    const bool hit = (res_hit[k] >> p) & 1u;
+                    spa += hit ? 0.0f : 1.0f;
+                    sta += hit ? res_t[k * TP + p] : c.spec_len;
+                }
+                sp = spa / (float)c.n_spec;
+                st = sta / (float)c.n_spec;
+            }
+        }
+        if (S.o_shadow) S.o_shadow[gpix] = sh;
+        if (S.o_ao) S.o_ao[gpix] = ao;
+        if (S.o_vis) S.o_vis[gpix] = vis;
+        if (S.o_spec) S.o_spec[gpix] = sp;
+        if (S.o_spec_t) S.o_spec_t[gpix] = st;
+    }
+    __syncwarp();
+}
+
 #ifndef VXL_POOL_MIN_BLOCKS
 #define VXL_POOL_MIN_BLOCKS 8  // 8 blocks of 4 warps: 64 registers per thread
 #endif
+
+// one scene; its descriptor lives in kernel parameter space
 template <int TP, int KSTEP, bool LEAP, bool RECORDS>
-__global__ void __launch_bounds__(128, VXL_POOL_MIN_BLOCKS) k_occl_pool(GridView g, const float* __restrict__ pos,
-                                                   const float* __restrict__ nrm, const float* __restrict__ rough,
-                                                   int64_t npix, TraceConstsP c, float* __restrict__ o_shadow,
-                                                   float* __restrict__ o_ao, float* __restrict__ o_vis,
-                                                   float* __restrict__ o_spec, float* __restrict__ o_spec_t,
-                                                   vxl_ray_record* __restrict__ rec, int* __restrict__ tile_counter) {
-    constexpr int LPP = 32 / TP;  // lanes per pixel during generation
+__global__ void __launch_bounds__(128, VXL_POOL_MIN_BLOCKS) k_occl_pool(const SceneDesc S, unsigned long long* __restrict__ counter,
+                                                                        int grab) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const int R = c.R;
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    unsigned char* wbase = smem + warp * pool_bytes(TP, R);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned char* wbase = smem + warp * pool_bytes(TP, S.c.R);
     PSlot* slots = reinterpret_cast<PSlot*>(wbase);
-    float* res_t = reinterpret_cast<float*>(wbase + (size_t)TP * R * sizeof(PSlot));
-    uint32_t* res_hit = reinterpret_cast<uint32_t*>(wbase + (size_t)TP * R * (sizeof(PSlot) + sizeof(float)));
-    const unsigned lt_mask = (1u << lane) - 1u;
-    const int64_t ntiles = (npix + TP - 1) / TP;
-    const unsigned ux = (unsigned)g.nx + 1u, uy = (unsigned)g.ny + 1u, uz = (unsigned)g.nz + 1u;
-
+    float* res_t = reinterpret_cast<float*>(wbase + (size_t)TP * S.c.R * sizeof(PSlot));
+    uint32_t* res_hit = reinterpret_cast<uint32_t*>(wbase + (size_t)TP * S.c.R * (sizeof(PSlot) + sizeof(float)));
+    const GridView g = S.g;
     for (;;) {
-        int tile = 0;
-        if (lane == 0) tile = atomicAdd(tile_counter, 1);
-        tile = __shfl_sync(0xffffffffu, tile, 0);
-        if (tile >= ntiles) break;
-
-        // ---------------------------------------------------------- A
-        const int p = lane % TP;
-        const int64_t gpix = (int64_t)tile * TP + p;
-        const bool inimg = gpix < npix;
-        f3 P = mk(0.0f, 0.0f, 0.0f), N = mk(0.0f, 0.0f, 0.0f);
-        float ro = c.default_rough;
-        if (inimg) {
-            P = ld3(pos + 3 * gpix);
-            N = ld3(nrm + 3 * gpix);
-            if (rough) ro = rough[gpix];
-        }
-        const bool sky = !inimg || (N.x == 0.0f && N.y == 0.0f && N.z == 0.0f);
-        f3 O = add(P, mul(N, c.bias));
-        f3 T, B;
-        tangent_frame(N, &T, &B);
-        for (int k = lane; k < R; k += 32) res_hit[k] = 0u;
-        int live = 0;
-        const int rounds = (R + LPP - 1) / LPP;
-        for (int j = 0; j < rounds; j++) {
-            // generation (= dispatch) order: spec rays first, then shadow, then
-            // AO, so the longest rays start early and the pool drains on short ones
-            const int kk = j * LPP + lane / TP;
-            const int k = !c.spec_first ? kk : (kk < c.n_spec ? c.n_shadow + c.n_ao + kk : kk - c.n_spec);
-            bool is_live = false;
-            PSlot sl;
-            if (kk < R && !sky) {
-                f3 d = gen_dir(c, k, (uint32_t)gpix, P, N, T, B, ro);
-                float maxt = kind_maxt(c, k);
-                int meta = (p << 4) | (k << 9);
-                Hit h0{0, 0, 0, 0.0f, 0, VXL_RF_EXIT_BOUNDS};
-                bool born_done = false;
-                if (!ray_domain_ok(O, d)) {
-                    born_done = true;
-                } else if (!dir_fast_ok(d)) {
-                    is_live = true;
-                    sl.c01 = 0;
-                    sl.c2m = (meta | kMetaLit) << 16;
-                    sl.a0 = O.x; sl.a1 = O.y; sl.a2 = O.z;
-                    sl.b0 = d.x; sl.b1 = d.y; sl.b2 = d.z;
-                } else {
-                    DState s;
-                    dda_init(s, O, d, maxt);
-                    if ((unsigned)s.cx > ux || (unsigned)s.cy > uy || (unsigned)s.cz > uz) {
-                        born_done = true;  // origin cell out of bounds: the first test exits (Light.frag:53)
-                        h0 = Hit{s.cx, s.cy, s.cz, 0.0f, 0, VXL_RF_EXIT_BOUNDS};
-                    } else {
-                        is_live = true;
-                        meta |= (s.sx < 0 ? 1 : 0) | (s.sy < 0 ? 2 : 0) | (s.sz < 0 ? 4 : 0);
-                        if (LEAP && !RECORDS && leap_allowed(d, maxt)) meta |= kMetaLeap;
-                        sl.c01 = (s.cx & 0xffff) | (s.cy << 16);
-                        sl.c2m = (s.cz & 0xffff) | (meta << 16);
-                        sl.a0 = s.tx; sl.a1 = s.ty; sl.a2 = s.tz;
-                        sl.b0 = s.tdx; sl.b1 = s.tdy; sl.b2 = s.tdz;
-                    }
-                }
-                if (born_done) {
-                    res_t[k * TP + p] = h0.t;
-                    if (RECORDS) store_record(rec + gpix * R + k, h0);
-                }
-            } else if (kk < R && RECORDS && inimg) {
-                Hit z{0, 0, 0, 0.0f, 0, 0};
-                store_record(rec + gpix * R + k, z);
-            }
-            const unsigned lv = __ballot_sync(0xffffffffu, is_live);
-            if (is_live) {
-                const int at = live + __popc(lv & lt_mask);
-                slots[at] = sl;
-            }
-            live += __popc(lv);
-        }
-        __syncwarp();
-
-        // ---------------------------------------------------------- B
-        int base = 0;
-        int my = -1;
-        bool retired = false;
-        DState s;
-        int meta = 0;
-        for (;;) {
-            const bool need = my < 0 && !retired;
-            const unsigned nm = __ballot_sync(0xffffffffu, need);
-            if (nm) {
-                if (need) {
-                    const int at = base + __popc(nm & lt_mask);
-                    if (at < live) {
-                        const PSlot sl = slots[at];
-                        meta = (unsigned)sl.c2m >> 16;
-                        const int k = (meta >> 9) & 31;
-                        const float maxt = kind_maxt(c, k);
-                        if (meta & kMetaLit) {
-                            Hit h = dda_literal(g, mk(sl.a0, sl.a1, sl.a2), mk(sl.b0, sl.b1, sl.b2), maxt);
-                            const int pp = (meta >> 4) & 31;
-                            res_t[k * TP + pp] = h.t;
-                            if (h.flags & VXL_RF_HIT) atomicOr(&res_hit[k], 1u << pp);
-                            if (RECORDS) store_record(rec + ((int64_t)tile * TP + pp) * R + k, h);
-                        } else {
-                            my = at;
-                            s.cx = lo16(sl.c01);
-                            s.cy = hi16(sl.c01);
-                            s.cz = lo16(sl.c2m);
-                            s.tx = sl.a0; s.ty = sl.a1; s.tz = sl.a2;
-                            s.tdx = sl.b0; s.tdy = sl.b1; s.tdz = sl.b2;
-                            s.sx = (meta & 1) ? -1 : 1;
-                            s.sy = (meta & 2) ? -1 : 1;
-                            s.sz = (meta & 4) ? -1 : 1;
-                            s.maxt = maxt;
-                            s.tot = 0.0f;
-                            s.n = 0;
-                            s.leap = (meta & kMetaLeap) != 0;
-                            s.wcur = 0xffffffffu;
-                            s.word = 0;
-                        }
-                    } else {
-                        retired = true;
-                    }
-                }
-                base += __popc(nm);
-            }
-            if (!__any_sync(0xffffffffu, my >= 0) && base >= live) break;
-            if (my >= 0) {
-                Hit h;
-                const int f = dda_run<LEAP>(g, s, h, KSTEP);
-                if (f) {
-                    const int k = (meta >> 9) & 31, pp = (meta >> 4) & 31;
-                    res_t[k * TP + pp] = h.t;
-                    if (f & VXL_RF_HIT) atomicOr(&res_hit[k], 1u << pp);
-                    if (RECORDS) store_record(rec + ((int64_t)tile * TP + pp) * R + k, h);
-                    my = -1;
-                }
-            }
-        }
-        __syncwarp();
-
-        // ---------------------------------------------------------- C
-        if (lane < TP && inimg) {
-            float sh = 1.0f, ao = 1.0f, vis = 1.0f, sp = 1.0f, st = c.spec_len;
-            if (!sky) {
-                int k = 0;
-                if (c.n_shadow > 0) {
-                    sh = ((res_hit[0] >> p) & 1u) ? 0.0f : 1.0f;
-                    k = 1;
-                }
-                float acc = 0.0f, v = 0.0f;
-                for (int j = 0; j < c.n_ao; j++, k++) {
-                    const bool hit = (res_hit[k] >> p) & 1u;
-                    const float t = res_t[k * TP + p];
-                    float tt = hit ? (t < c.ao_len ? t : c.ao_len) : c.ao_len;
-                    float q = tt / c.ao_len;
-                    acc += q * q;
-                    v += hit ? 0.0f : 1.0f;
-                }
-                if (c.n_ao > 0) {
-                    ao = acc / (float)c.n_ao;
-                    vis = v / (float)c.n_ao;
-                }
-                if (c.n_spec > 0) {
-                    float spa = 0.0f, sta = 0.0f;
-                    for (int j = 0; j < c.n_spec; j++, k++) {
-                        const bool hit = (res_hit[k] >> p) & 1u;
-                        spa += hit ? 0.0f : 1.0f;
-                        sta += hit ? res_t[k * TP + p] : c.spec_len;
-                    }
-                    sp = spa / (float)c.n_spec;
-                    st = sta / (float)c.n_spec;
-                }
-            }
-            if (o_shadow) o_shadow[gpix] = sh;
-            if (o_ao) o_ao[gpix] = ao;
-            if (o_vis) o_vis[gpix] = vis;
-            if (o_spec) o_spec[gpix] = sp;
-            if (o_spec_t) o_spec_t[gpix] = st;
-        }
-        __syncwarp();
+        int64_t t0 = 0;
+        if (lane == 0) t0 = (int64_t)atomicAdd(counter, (unsigned long long)grab);
+        t0 = __shfl_sync(0xffffffffu, t0, 0);
+        if (t0 >= S.ntiles) break;
+        for (int64_t t = t0; t < t0 + grab && t < S.ntiles; t++)
+            process_tile<TP, KSTEP, LEAP, RECORDS>(S, g, t, slots, res_t, res_hit, lane);
     }
 }
 
-// ---------------------------------------------------------------- launcher
-constexpr int kPoolMaxR = 31;
-
-template <int TP, int KSTEP, bool LEAP, bool REC>
-static vxl_status launch_pool_t(vxl_ctx* ctx, GridView v, const vxl_gbuffer* gb, const TraceConstsP& c,
-                                const vxl_outputs* out, int* counter, cudaStream_t s) {
-    const int warps = 4;
-    size_t smem = pool_bytes(TP, c.R) * warps;
-    auto kern = k_occl_pool<TP, KSTEP, LEAP, REC>;
-    VXL_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per_sm = 0;
-    VXL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem));
-    if (per_sm < 1) return fail(VXL_ERR_NOT_SUPPORTED, "occlusion pool: %zu bytes of shared memory per block", smem);
-    int64_t tiles = (gb->npix + TP - 1) / TP;
-    int64_t blocks = (int64_t)ctx->sm_count * per_sm;
-    if (blocks * warps > tiles) blocks = (tiles + warps - 1) / warps;
-    kern<<<(unsigned)blocks, warps * 32, smem, s>>>(v, gb->pos, gb->nrm, gb->rough, gb->npix, c, out->shadow, out->ao,
-                                                   out->ao_vis, out->spec, out->spec_t, out->records, counter);
-    ctx->launches++;
-    VXL_TRY_CUDA(cudaGetLastError());
-    return VXL_OK;
-}
-
-template <int TP, bool LEAP>
-static vxl_status launch_pool_k(vxl_ctx* ctx, GridView v, const vxl_gbuffer* gb, const TraceConstsP& c,
-                                const vxl_outputs* out, int* counter, int kstep, cudaStream_t s) {
-    switch (kstep) {
-        case 1: return launch_pool_t<TP, 1, LEAP, false>(ctx, v, gb, c, out, counter, s);
-        case 2: return launch_pool_t<TP, 2, LEAP, false>(ctx, v, gb, c, out, counter, s);
-        case 8: return launch_pool_t<TP, 8, LEAP, false>(ctx, v, gb, c, out, counter, s);
-        default: return launch_pool_t<TP, 4, LEAP, false>(ctx, v, gb, c, out, counter, s);
+// many scenes, one counter over all their tiles (work stealing across scenes);
+// tiles are numbered scene after scene, table[i].tile_begin ascending
+template <int TP, int KSTEP, bool LEAP>
+__global__ void __launch_bounds__(128, VXL_POOL_MIN_BLOCKS) k_occl_batch(const SceneDesc* __restrict__ table,
+                                                                         int nscenes, int64_t total_tiles,
+                                                                         int max_r, unsigned long long* __restrict__ counter,
+                                                                         int grab) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned char* wbase = smem + warp * pool_bytes(TP, max_r);
+    for (;;) {
+        int64_t t0 = 0;
+        if (lane == 0) t0 = (int64_t)atomicAdd(counter, (unsigned long long)grab);
+        t0 = __shfl_sync(0xffffffffu, t0, 0);
+        if (t0 >= total_tiles) break;
+        for (int64_t t = t0; t < t0 + grab && t < total_tiles; t++) {
+            int lo = 0, hi = nscenes - 1;  // last scene with tile_begin <= t
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (table[mid].tile_begin <= t) lo = mid; else hi = mid - 1;
+            }
+            const SceneDesc& S = table[lo];
+            const int R = S.c.R;
+            PSlot* slots = reinterpret_cast<PSlot*>(wbase);
+            float* res_t = reinterpret_cast<float*>(wbase + (size_t)TP * R * sizeof(PSlot));
+            uint32_t* res_hit = reinterpret_cast<uint32_t*>(wbase + (size_t)TP * R * (sizeof(PSlot) + sizeof(float)));
+            const GridView g = S.g;
+            process_tile<TP, KSTEP, LEAP, false>(S, g, t - S.tile_begin, slots, res_t, res_hit, lane);
+        }
     }
 }
 
-bool occl_pool_supported(const vxl_grid* g, const vxl_trace_params* p) {
-    int R = p->n_shadow + p->n_ao + p->n_spec;
-    // 16-bit packed cells hold [-1, n+2]
-    return R >= 1 && R <= kPoolMaxR && g->nx <= 32760 && g->ny <= 32760 && g->nz <= 32760;
-}
-
-vxl_status launch_trace_occlusion_pool(vxl_ctx* ctx, const vxl_grid* g, const vxl_gbuffer* gb,
-                                       const vxl_trace_params* p, const vxl_outputs* out, int* d_counter,
-                                       const vxl_tuning& tune, cudaStream_t s) {
+// ---------------------------------------------------------------- host side
+static TraceConstsP consts_of(const vxl_trace_params* p, const vxl_tuning& tune) {
     TraceConstsP c;
     c.light = mk(p->light_dir[0], p->light_dir[1], p->light_dir[2]);
     c.cam = mk(p->cam_pos[0], p->cam_pos[1], p->cam_pos[2]);
@@ -337,19 +378,164 @@ vxl_status launch_trace_occlusion_pool(vxl_ctx* ctx, const vxl_grid* g, const vx
     c.R = p->n_shadow + p->n_ao + p->n_spec;
     c.seed_h = pcg(p->seed);
     c.spec_first = tune.order == 1;
-    GridView v = view_of(g);
-    VXL_TRY_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(int), s));
+    return c;
+}
+
+// scene descriptor and its tile count for the given tile size / shape
+static SceneDesc scene_of(const vxl_grid* g, const vxl_gbuffer* gb, const vxl_trace_params* p, const vxl_outputs* o,
+                          const vxl_tuning& tune) {
+    SceneDesc S;
+    S.g = view_of(g);
+    S.pos = gb->pos;
+    S.nrm = gb->nrm;
+    S.rough = gb->rough;
+    S.o_shadow = o->shadow;
+    S.o_ao = o->ao;
+    S.o_vis = o->ao_vis;
+    S.o_spec = o->spec;
+    S.o_spec_t = o->spec_t;
+    S.rec = o->records;
+    S.npix = gb->npix;
+    S.tile_begin = 0;
+    S.pad = 0;
+    const int TP = tune.tile_px;
+    S.tile_w = TP;
+    S.width = S.height = 0;
+    if (tune.tile_w > 0 && tune.tile_w < TP && gb->width > 0 && gb->height > 0 &&
+        (int64_t)gb->width * gb->height == gb->npix) {
+        S.tile_w = tune.tile_w;
+        S.width = gb->width;
+        S.height = gb->height;
+        const int th = TP / tune.tile_w;
+        S.ntiles = (int64_t)((gb->width + tune.tile_w - 1) / tune.tile_w) * ((gb->height + th - 1) / th);
+    } else {
+        S.ntiles = (gb->npix + TP - 1) / TP;
+    }
+    S.c = consts_of(p, tune);
+    return S;
+}
+
+template <typename K>
+static vxl_status blocks_for_kernel(vxl_ctx* ctx, K kern, size_t smem, int* blocks_per_sm) {
+    VXL_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    VXL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kern, 128, smem));
+    if (*blocks_per_sm < 1)
+        return fail(VXL_ERR_NOT_SUPPORTED, "occlusion pool: %zu bytes of shared memory per block", smem);
+    return VXL_OK;
+}
+
+template <int TP, int KSTEP, bool LEAP, bool REC>
+static vxl_status launch_pool_t(vxl_ctx* ctx, const SceneDesc& S, unsigned long long* counter, int grab,
+                                cudaStream_t s) {
+    const size_t smem = pool_bytes(TP, S.c.R) * 4;
+    auto kern = k_occl_pool<TP, KSTEP, LEAP, REC>;
+    int per_sm = 0;
+    VXL_TRY(blocks_for_kernel(ctx, kern, smem, &per_sm));
+    int64_t blocks = (int64_t)ctx->sm_count * per_sm;
+    const int64_t warps_needed = (S.ntiles + grab - 1) / grab;
+    if (blocks * 4 > warps_needed) blocks = (warps_needed + 3) / 4;
+    kern<<<(unsigned)blocks, 128, smem, s>>>(S, counter, grab);
+    ctx->launches++;
+    VXL_TRY_CUDA(cudaGetLastError());
+    return VXL_OK;
+}
+
+template <int TP, bool LEAP>
+static vxl_status launch_pool_k(vxl_ctx* ctx, const SceneDesc& S, unsigned long long* counter, const vxl_tuning& t,
+                                cudaStream_t s) {
+    switch (t.kstep) {
+        case 1: return launch_pool_t<TP, 1, LEAP, false>(ctx, S, counter, t.grab, s);
+        case 2: return launch_pool_t<TP, 2, LEAP, false>(ctx, S, counter, t.grab, s);
+        case 4: return launch_pool_t<TP, 4, LEAP, false>(ctx, S, counter, t.grab, s);
+        default: return launch_pool_t<TP, 8, LEAP, false>(ctx, S, counter, t.grab, s);
+    }
+}
+
+bool occl_pool_supported(const vxl_grid* g, const vxl_trace_params* p) {
+    int R = p->n_shadow + p->n_ao + p->n_spec;
+    // 16-bit packed cells hold [-1, n+2]
+    return R >= 1 && R <= kPoolMaxR && g->nx <= 32760 && g->ny <= 32760 && g->nz <= 32760;
+}
+
+vxl_status launch_trace_occlusion_pool(vxl_ctx* ctx, const vxl_grid* g, const vxl_gbuffer* gb,
+                                       const vxl_trace_params* p, const vxl_outputs* out,
+                                       unsigned long long* d_counter, const vxl_tuning& tune, cudaStream_t s) {
+    const SceneDesc S = scene_of(g, gb, p, out, tune);
+    VXL_TRY_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s));
     // per-ray records need the exact iteration count: no leaps there
     if (out->records) {
-        if (tune.tile_px == 16) return launch_pool_t<16, 4, false, true>(ctx, v, gb, c, out, d_counter, s);
-        return launch_pool_t<32, 4, false, true>(ctx, v, gb, c, out, d_counter, s);
+        if (tune.tile_px == 16) return launch_pool_t<16, 4, false, true>(ctx, S, d_counter, tune.grab, s);
+        return launch_pool_t<32, 4, false, true>(ctx, S, d_counter, tune.grab, s);
     }
     if (tune.leap == 1) {
-        if (tune.tile_px == 16) return launch_pool_k<16, true>(ctx, v, gb, c, out, d_counter, tune.kstep, s);
-        return launch_pool_k<32, true>(ctx, v, gb, c, out, d_counter, tune.kstep, s);
+        if (tune.tile_px == 16) return launch_pool_k<16, true>(ctx, S, d_counter, tune, s);
+        return launch_pool_k<32, true>(ctx, S, d_counter, tune, s);
     }
-    if (tune.tile_px == 16) return launch_pool_k<16, false>(ctx, v, gb, c, out, d_counter, tune.kstep, s);
-    return launch_pool_k<32, false>(ctx, v, gb, c, out, d_counter, tune.kstep, s);
+    if (tune.tile_px == 16) return launch_pool_k<16, false>(ctx, S, d_counter, tune, s);
+    return launch_pool_k<32, false>(ctx, S, d_counter, tune, s);
+}
+
+// ------------------------------------------------------------------ batch
+struct BatchPlan {
+    SceneDesc* d_table;
+    int n;
+    int max_r;
+    int64_t total_tiles;
+    vxl_tuning tune;
+    unsigned long long* counter;
+};
+
+template <int TP, int KSTEP>
+static vxl_status launch_batch_t(vxl_ctx* ctx, const BatchPlan& b, cudaStream_t s) {
+    const size_t smem = pool_bytes(TP, b.max_r) * 4;
+    auto kern = k_occl_batch<TP, KSTEP, false>;
+    int per_sm = 0;
+    VXL_TRY(blocks_for_kernel(ctx, kern, smem, &per_sm));
+    int64_t blocks = (int64_t)ctx->sm_count * per_sm;
+    const int64_t warps_needed = (b.total_tiles + b.tune.grab - 1) / b.tune.grab;
+    if (blocks * 4 > warps_needed) blocks = (warps_needed + 3) / 4;
+    kern<<<(unsigned)blocks, 128, smem, s>>>(b.d_table, b.n, b.total_tiles, b.max_r, b.counter, b.tune.grab);
+    ctx->launches++;
+    VXL_TRY_CUDA(cudaGetLastError());
+    return VXL_OK;
+}
+
+template <int TP>
+static vxl_status launch_batch_k(vxl_ctx* ctx, const BatchPlan& b, cudaStream_t s) {
+    switch (b.tune.kstep) {
+        case 1: return launch_batch_t<TP, 1>(ctx, b, s);
+        case 2: return launch_batch_t<TP, 2>(ctx, b, s);
+        case 4: return launch_batch_t<TP, 4>(ctx, b, s);
+        default: return launch_batch_t<TP, 8>(ctx, b, s);
+    }
+}
+
+size_t batch_desc_bytes() { return sizeof(SceneDesc); }
+
+vxl_status batch_build_table(const vxl_batch_item* items, int n, const vxl_tuning& tune, void* h_table, int* max_r,
+                             int64_t* total_tiles, int64_t* total_rays) {
+    SceneDesc* t = (SceneDesc*)h_table;
+    int64_t tiles = 0, rays = 0;
+    int mr = 1;
+    for (int i = 0; i < n; i++) {
+        t[i] = scene_of(items[i].grid, &items[i].gbuf, &items[i].params, &items[i].out, tune);
+        t[i].tile_begin = tiles;
+        tiles += t[i].ntiles;
+        rays += items[i].gbuf.npix * t[i].c.R;
+        if (t[i].c.R > mr) mr = t[i].c.R;
+    }
+    *max_r = mr;
+    *total_tiles = tiles;
+    *total_rays = rays;
+    return VXL_OK;
+}
+
+vxl_status launch_batch(vxl_ctx* ctx, void* d_table, int n, int max_r, int64_t total_tiles, const vxl_tuning& tune,
+                        unsigned long long* d_counter, cudaStream_t s) {
+    BatchPlan b{(SceneDesc*)d_table, n, max_r, total_tiles, tune, d_counter};
+    VXL_TRY_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s));
+    if (tune.tile_px == 16) return launch_batch_k<16>(ctx, b, s);
+    return launch_batch_k<32>(ctx, b, s);
 }
 
 }  // namespace vxl

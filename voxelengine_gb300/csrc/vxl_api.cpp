@@ -55,7 +55,7 @@ vxl_status ctx_stage(vxl_ctx* ctx, size_t bytes, void** out) {
     return VXL_OK;
 }
 
-int* ctx_next_counter(vxl_ctx* ctx) { return ctx->d_counters + (ctx->counter_next++ % kCounterRing); }
+unsigned long long* ctx_next_counter(vxl_ctx* ctx) { return ctx->d_counters + (ctx->counter_next++ % kCounterRing); }
 
 // glm::translate(m, v): Result[3] = m[0]*v[0] + m[1]*v[1] + m[2]*v[2] + m[3]
 static void translate(const float* m, const float* v, float* out) {
@@ -193,14 +193,14 @@ vxl_status vxl_ctx_create(int device, vxl_ctx** out) {
     if (!c) return fail(VXL_ERR_OOM, "ctx_create: host allocation");
     c->device = device;
     e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
-    if (e == cudaSuccess) e = cudaMalloc(&c->d_counters, kCounterRing * sizeof(int));
-    if (e == cudaSuccess) e = cudaMemset(c->d_counters, 0, kCounterRing * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_counters, kCounterRing * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(c->d_counters, 0, kCounterRing * sizeof(unsigned long long));
     if (e != cudaSuccess) {
         if (c->d_counters) cudaFree(c->d_counters);
         delete c;
         return cuda_fail(e, "ctx_create");
     }
-    c->tune = vxl_tuning{16, 8, 2, 1};  // best on GB300 for the 512^3 / 1080p workload
+    c->tune = vxl_tuning{16, 8, 2, 1, 16, 1};  // best on GB300 for the 512^3 / 1080p workload
     *out = c;
     return VXL_OK;
 }
@@ -241,6 +241,14 @@ vxl_status vxl_ctx_set_tuning(vxl_ctx* ctx, const vxl_tuning* t) {
         if (t->order != 1 && t->order != 2) return fail(VXL_ERR_INVALID_ARG, "order must be 1 or 2");
         n.order = t->order;
     }
+    if (t->grab) {
+        if (t->grab != 1 && t->grab != 2 && t->grab != 4) return fail(VXL_ERR_INVALID_ARG, "grab must be 1, 2 or 4");
+        n.grab = t->grab;
+    }
+    if (t->tile_w) n.tile_w = t->tile_w;
+    if (n.tile_w > n.tile_px || n.tile_px % n.tile_w != 0 ||
+        (n.tile_w != n.tile_px && n.tile_w != 4 && n.tile_w != 8))
+        n.tile_w = n.tile_px;  // shapes that do not divide the tile fall back to pixel runs
     ctx->tune = n;
     return VXL_OK;
 }
@@ -419,6 +427,114 @@ vxl_status vxl_trace_occlusion_host(vxl_ctx* ctx, const vxl_grid* g, const float
     for (int k = 0; k < 5; k++)
         if (hs[k]) VXL_TRY_CUDA(cudaMemcpyAsync(hs[k], outs[k], b1, cudaMemcpyDeviceToHost, s));
     VXL_TRY_CUDA(cudaStreamSynchronize(s));
+    return VXL_OK;
+}
+
+}  // extern "C"
+
+struct vxl_batch {
+    vxl_ctx* ctx;
+    void* d_table;
+    unsigned long long* d_counter;
+    int n, max_r;
+    int64_t tiles, rays;
+    vxl_tuning tune;
+    cudaStream_t cap_stream;
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+};
+
+extern "C" {
+
+vxl_status vxl_batch_create(vxl_ctx* ctx, const vxl_batch_item* items, int n, int use_graph, vxl_batch** out) {
+    if (!ctx || !out || n <= 0 || !items) return fail(VXL_ERR_INVALID_ARG, "batch_create: bad argument");
+    *out = nullptr;
+    for (int i = 0; i < n; i++) {
+        const vxl_batch_item& it = items[i];
+        if (!grid_ok(it.grid)) return fail(VXL_ERR_INVALID_ARG, "batch item %d: bad grid", i);
+        if (it.grid->ctx != ctx) return fail(VXL_ERR_INVALID_ARG, "batch item %d: grid of another context", i);
+        VXL_TRY(check_params(&it.params));
+        if (it.gbuf.npix < 0 || (it.gbuf.npix > 0 && (!it.gbuf.pos || !it.gbuf.nrm)))
+            return fail(VXL_ERR_INVALID_ARG, "batch item %d: bad G-buffer", i);
+        if (it.out.records) return fail(VXL_ERR_INVALID_ARG, "batch item %d: records are not supported in a batch", i);
+        if (!occl_pool_supported(it.grid, &it.params))
+            return fail(VXL_ERR_NOT_SUPPORTED, "batch item %d: more than 31 rays per pixel or grid above 32760", i);
+    }
+    VXL_TRY(set_device(ctx));
+    vxl_batch* b = new (std::nothrow) vxl_batch();
+    if (!b) return fail(VXL_ERR_OOM, "batch_create: host allocation");
+    b->ctx = ctx;
+    b->n = n;
+    b->tune = ctx->tune;
+    std::vector<unsigned char> table((size_t)n * batch_desc_bytes());
+    batch_build_table(items, n, b->tune, table.data(), &b->max_r, &b->tiles, &b->rays);
+    auto cleanup = [b]() {
+        if (b->exec) cudaGraphExecDestroy(b->exec);
+        if (b->graph) cudaGraphDestroy(b->graph);
+        if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+        if (b->d_table) cudaFree(b->d_table);
+        if (b->d_counter) cudaFree(b->d_counter);
+        delete b;
+    };
+    cudaError_t e = cudaMalloc(&b->d_table, table.size());
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_counter, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_table, table.data(), table.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cleanup();
+        return cuda_fail(e, "batch_create: device table");
+    }
+    if (use_graph) {
+        e = cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeRelaxed);
+        if (e != cudaSuccess) {
+            cleanup();
+            return cuda_fail(e, "batch_create: begin capture");
+        }
+        vxl_status st = launch_batch(ctx, b->d_table, n, b->max_r, b->tiles, b->tune, b->d_counter, b->cap_stream);
+        ctx->launches--;  // captured, not run
+        e = cudaStreamEndCapture(b->cap_stream, &b->graph);
+        if (st != VXL_OK || e != cudaSuccess) {
+            cleanup();
+            return st != VXL_OK ? st : cuda_fail(e, "batch_create: end capture");
+        }
+        e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+        if (e != cudaSuccess) {
+            cleanup();
+            return cuda_fail(e, "batch_create: graph instantiate");
+        }
+    }
+    *out = b;
+    return VXL_OK;
+}
+
+vxl_status vxl_batch_run(vxl_batch* b, void* stream) {
+    if (!b) return fail(VXL_ERR_INVALID_ARG, "batch_run: NULL batch");
+    VXL_TRY(set_device(b->ctx));
+    cudaStream_t s = (cudaStream_t)stream;
+    if (b->exec) {
+        VXL_TRY_CUDA(cudaGraphLaunch(b->exec, s));
+        b->ctx->launches++;
+        return VXL_OK;
+    }
+    return launch_batch(b->ctx, b->d_table, b->n, b->max_r, b->tiles, b->tune, b->d_counter, s);
+}
+
+vxl_status vxl_batch_destroy(vxl_batch* b) {
+    if (!b) return VXL_OK;
+    cudaSetDevice(b->ctx->device);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+    cudaFree(b->d_table);
+    cudaFree(b->d_counter);
+    delete b;
+    return VXL_OK;
+}
+
+vxl_status vxl_batch_info(const vxl_batch* b, int64_t* tiles, int64_t* rays) {
+    if (!b) return fail(VXL_ERR_INVALID_ARG, "batch_info: NULL batch");
+    if (tiles) *tiles = b->tiles;
+    if (rays) *rays = b->rays;
     return VXL_OK;
 }
 

@@ -20,7 +20,7 @@ struct vxl_ctx {
     // ring of work-queue counters for the persistent kernels: each launch
     // takes the next one, so launches in flight on different streams never
     // share a counter
-    int* d_counters;
+    unsigned long long* d_counters;
     uint32_t counter_next;
     vxl_tuning tune;  // occlusion kernel launch shape (vxl_ctx_set_tuning)
 };
@@ -86,9 +86,15 @@ vxl_status launch_trace_occlusion(vxl_ctx* ctx, const vxl_grid* g, const vxl_gbu
                                   const vxl_outputs* out, cudaStream_t s);
 bool occl_pool_supported(const vxl_grid* g, const vxl_trace_params* p);
 vxl_status launch_trace_occlusion_pool(vxl_ctx* ctx, const vxl_grid* g, const vxl_gbuffer* gb,
-                                       const vxl_trace_params* p, const vxl_outputs* out, int* d_counter,
-                                       const vxl_tuning& tune, cudaStream_t s);
-int* ctx_next_counter(vxl_ctx* ctx);
+                                       const vxl_trace_params* p, const vxl_outputs* out,
+                                       unsigned long long* d_counter, const vxl_tuning& tune, cudaStream_t s);
+unsigned long long* ctx_next_counter(vxl_ctx* ctx);
+// batched occlusion: scene table built on the host, uploaded once, one launch
+size_t batch_desc_bytes();
+vxl_status batch_build_table(const vxl_batch_item* items, int n, const vxl_tuning& tune, void* h_table, int* max_r,
+                             int64_t* total_tiles, int64_t* total_rays);
+vxl_status launch_batch(vxl_ctx* ctx, void* d_table, int n, int max_r, int64_t total_tiles, const vxl_tuning& tune,
+                        unsigned long long* d_counter, cudaStream_t s);
 vxl_status launch_light_ambient(vxl_ctx* ctx, const vxl_grid* g, const float* wcp, const float* nrm,
                                 const float* depth, const float* noise, int64_t npix, float* shadow, float* irr,
                                 vxl_ray_record* rec, cudaStream_t s);

@@ -1,0 +1,129 @@
+"""Seeded synthetic scene sets for benchmarks and tests (device-generated).
+
+A scene is a noise grid (3-octave value noise at frequency 1/32, threshold
+`thresh`, ground slab y < 8), optional boxes and voxelized Vox-model
+instances, and a primary-hit G-buffer from a camera outside the grid looking
+at its centre. Device buffers are torch CUDA tensors.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+import voxelengine_gb300 as V
+
+
+def camera(n):
+    """Above and in front of an n^3 grid, looking at its centre."""
+    cam = np.array([0.5 * n, 1.15 * n, -0.1 * n], np.float32)
+    tgt = np.array([0.5 * n, 0.5 * n, 0.5 * n], np.float32)
+    return cam, tgt
+
+
+def light_dir(seed):
+    rng = np.random.default_rng(seed)
+    v = rng.normal(size=3)
+    v[1] = abs(v[1]) + 0.8  # above the horizon
+    return (v / np.linalg.norm(v)).astype(np.float32)
+
+
+def image_for_pixels(npix):
+    """16:9-ish W x H with about npix pixels."""
+    h = max(8, int(round(math.sqrt(npix * 9.0 / 16.0))))
+    w = max(8, int(round(npix / h)))
+    return w, h
+
+
+def rotation_matrix(rng):
+    """Uniform random rotation (unit quaternion from three uniforms, Shoemake)."""
+    u1, u2, u3 = rng.random(3)
+    x = math.sqrt(1 - u1) * math.sin(2 * math.pi * u2)
+    y = math.sqrt(1 - u1) * math.cos(2 * math.pi * u2)
+    z = math.sqrt(u1) * math.sin(2 * math.pi * u3)
+    w = math.sqrt(u1) * math.cos(2 * math.pi * u3)
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def vox_models(seed, count, edge_min=8, edge_max=64, fill=0.4):
+    """Dense uint8 palette blocks [sz, sy, sx]: opaque indices 16..255 with
+    probability `fill`, a few glass indices 1..15, zeros elsewhere."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        sx, sy, sz = (int(v) for v in rng.integers(edge_min, edge_max + 1, 3))
+        m = rng.integers(16, 256, (sz, sy, sx)).astype(np.uint8)
+        m[rng.random((sz, sy, sx)) >= fill] = 0
+        glass = rng.random((sz, sy, sx)) < 0.02
+        m[glass] = rng.integers(1, 16, int(glass.sum())).astype(np.uint8)
+        out.append(m)
+    return out
+
+
+def instance_matrix(rng, n, model_shape):
+    """Column-major 4x4: uniform rotation, model centre inside an n^3 grid
+    (positions in world units: 10 fine voxels per unit)."""
+    m = np.eye(4)
+    R = rotation_matrix(rng)
+    m[:3, :3] = R
+    sz, sy, sx = model_shape
+    half = 0.05 * np.array([sx, sy, sz])  # model half extent in world units
+    centre = rng.uniform(0.0, n / 10.0, 3)
+    m[:3, 3] = centre - R @ half
+    return np.ascontiguousarray(m.T.astype(np.float32)).reshape(16)
+
+
+def make_scene(ctx, n, W, H, seed, thresh=0.55, boxes=0, params=None, device_tensors=True):
+    import torch
+
+    G = V.Grid(ctx, n, n, n)
+    G.scene_noise(seed, thresh, 1.0 / 32.0, 8)
+    if boxes:
+        G.scene_boxes(seed, boxes, 4, 48)
+    cam, tgt = camera(n)
+    npix = W * H
+    pos = torch.empty(npix * 3, dtype=torch.float32, device="cuda")
+    nrm = torch.empty_like(pos)
+    rough = torch.empty(npix, dtype=torch.float32, device="cuda")
+    V.scene_gbuffer(ctx, G, cam, tgt, W, H, seed, pos, nrm, rough)
+    P = params or V.make_params(light_dir=light_dir(seed), cam_pos=cam, bias=0.5, shadow_len=100.0, ao_len=32.0,
+                                spec_len=256.0, n_shadow=1, n_ao=8, n_spec=1, seed=seed)
+    return dict(grid=G, n=n, W=W, H=H, width=W, height=H, npix=npix, pos=pos, nrm=nrm, rough=rough, params=P,
+                cam=cam, seed=seed)
+
+
+def batch_set(ctx, count=64, seed=7, edge_range=(64, 512), rays_range=(64 * 1024, 2 * 1024 * 1024),
+              thresh_range=(0.45, 0.65), rays_per_pixel=10):
+    """The uneven scene mix: edges log-uniform in edge_range (even), noise
+    threshold uniform in thresh_range, rays per scene log-uniform in rays_range."""
+    rng = np.random.default_rng(seed)
+    scenes = []
+    for i in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(edge_range[0]), math.log(edge_range[1]))) / 2)) * 2
+        rays = math.exp(rng.uniform(math.log(rays_range[0]), math.log(rays_range[1])))
+        W, H = image_for_pixels(rays / rays_per_pixel)
+        thresh = float(rng.uniform(*thresh_range))
+        scenes.append(make_scene(ctx, n, W, H, seed * 1000 + i, thresh=thresh))
+    return scenes
+
+
+def add_outputs(scene):
+    import torch
+
+    for k in ("shadow", "ao", "ao_vis", "spec", "spec_t"):
+        scene[k] = torch.empty(scene["npix"], dtype=torch.float32, device="cuda")
+    return scene
+
+
+def instance_set(scenes, n_instances, models, seed):
+    """n_instances placements spread uniformly over the scenes: per scene a
+    list of (matrix16, model index, op)."""
+    rng = np.random.default_rng(seed)
+    per = [[] for _ in scenes]
+    for _ in range(n_instances):
+        s = int(rng.integers(0, len(scenes)))
+        mi = int(rng.integers(0, len(models)))
+        per[s].append((instance_matrix(rng, scenes[s]["n"], models[mi].shape), mi, V.OP_SET))
+    return per
