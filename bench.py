@@ -243,6 +243,9 @@ def run_gpu(args, wl):
     torch.cuda.set_device(local)
     V.build()
     ctx = V.Context(local)
+    from voxelengine_gb300 import autotune
+
+    autotune.apply_cached(ctx, args.workload)
     if args.tuning:
         ctx.set_tuning(*[int(x) for x in args.tuning.split(",")])
     n, W, H = wl["n"], wl["W"], wl["H"]
@@ -266,7 +269,7 @@ def run_gpu(args, wl):
 
     # per-ray fetch counts (S_ref) from one untimed pass with records
     rec = torch.empty(npix * R * 6, dtype=torch.int32, device="cuda")
-    V.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, records=rec, **outs)
+    V.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, records=rec, width=W, height=H, **outs)
     torch.cuda.synchronize()
     steps_col = rec.view(-1, 6)[:, 4].view(npix, R)
     vmask = (nrm.view(-1, 3).abs().sum(1) > 0)
@@ -274,6 +277,9 @@ def run_gpu(args, wl):
     hits = float(((rec.view(-1, 6)[:, 5] & 1).view(npix, R)[vmask]).double().mean().item())
     del rec
 
+    if args.autotune:
+        autotune.tune(ctx, lambda: (lambda: V.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, width=W, height=H, **outs)),
+                      args.workload, log=lambda m: print(m, file=sys.stderr))
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -282,7 +288,7 @@ def run_gpu(args, wl):
     # nvidia-smi query
     with ClockSampler(local) as clk:
         for _ in range(args.warmup):
-            V.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, **outs)
+            V.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, width=W, height=H, **outs)
         torch.cuda.synchronize()
         l0 = ctx.launch_count()
         barrier(dist)
@@ -290,7 +296,7 @@ def run_gpu(args, wl):
         for s in range(args.steps):
             flush.fill_(float(s))
             ev[s][0].record(stream)
-            V.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, **outs)
+            V.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, width=W, height=H, **outs)
             ev[s][1].record(stream)
         torch.cuda.synchronize()
         barrier(dist)
@@ -367,18 +373,114 @@ def run_gpu(args, wl):
     print(json.dumps(line))
 
 
+def run_gpu_c3(args):
+    """C3: 64 scenes (edges log-uniform 64-512, noise threshold U[0.45,0.65],
+    rays per scene log-uniform 64K-2M at 1 shadow + 8 AO + 1 spec per pixel),
+    10,000 Vox instances (edge 8-64, ~40% fill, uniform rotations) voxelized
+    into the scene grids first (timed on its own). One step = all 64 scenes:
+    the batched form (one persistent launch, CUDA-graph replay) against the
+    plain form (one vxl_trace_occlusion per scene)."""
+    import torch
+
+    import voxelengine_gb300 as V
+    from voxelengine_gb300 import scenes as S
+
+    V.build()
+    ctx = V.Context(0)
+    from voxelengine_gb300 import autotune
+
+    autotune.apply_cached(ctx, "c3")
+    if args.tuning:
+        ctx.set_tuning(*[int(x) for x in args.tuning.split(",")])
+    scenes = [S.add_outputs(sc) for sc in S.batch_set(ctx, 64, seed=7)]
+    models = S.vox_models(11, 32)
+    d_models = [torch.from_numpy(m).cuda() for m in models]
+    mdesc = [(d.data_ptr(),) + m.shape[::-1] for m, d in zip(models, d_models)]
+    per = S.instance_set(scenes, 10000, models, seed=13)
+    src_voxels = sum(int(np.prod(models[mi].shape)) for lst in per for _, mi, _ in lst)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for sc, lst in zip(scenes, per):
+        if lst:
+            V.voxelize(ctx, sc["grid"], mdesc, lst)
+    e1.record()
+    torch.cuda.synchronize()
+    t_vox = e0.elapsed_time(e1) / 1e3
+    # re-render the G-buffers now that the instances are in the grids
+    for sc in scenes:
+        V.scene_gbuffer(ctx, sc["grid"], sc["cam"], np.array([sc["n"] / 2] * 3, np.float32), sc["W"], sc["H"],
+                        sc["seed"], sc["pos"], sc["nrm"], sc["rough"])
+    rays = sum(sc["npix"] * 10 for sc in scenes)
+    valid = sum(int((sc["nrm"].view(-1, 3).abs().sum(1) > 0).sum().item()) for sc in scenes)
+    traced = valid * 10
+
+    def plain():
+        for sc in scenes:
+            V.trace_occlusion(ctx, sc["grid"], sc["pos"], sc["nrm"], sc["rough"], sc["npix"], sc["params"],
+                              shadow=sc["shadow"], ao=sc["ao"], ao_vis=sc["ao_vis"], spec=sc["spec"],
+                              spec_t=sc["spec_t"])
+
+    if args.autotune:
+        def make_step():
+            b = V.Batch(ctx, scenes, use_graph=True)
+            return b.run
+
+        autotune.tune(ctx, make_step, "c3", log=lambda m: print(m, file=sys.stderr))
+    batch = V.Batch(ctx, scenes, use_graph=True)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for s in range(args.steps):
+            flush.fill_(float(s))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            ts.append((a, b))
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in ts) / 1e3 / args.steps
+
+    with ClockSampler(0) as clk:
+        t_plain = timed(plain)
+        t_batch = timed(batch.run)
+    line = {
+        "metric": "Grays/s shadow+AO+spec occlusion, 64-scene batch (exact voxel DDA)",
+        "value": traced / t_batch / 1e9, "unit": "Grays/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_batch * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded scenes, G-buffers and Vox instances)",
+        "config": {"workload": "batch-64-scenes", "edges": [int(sc["n"]) for sc in scenes],
+                   "pixels": [int(sc["npix"]) for sc in scenes], "rays_per_pixel": 10, "instances": 10000,
+                   "l2": "flushed between timed steps"},
+        "plain_value": traced / t_plain / 1e9, "plain_ms_per_step": t_plain * 1e3,
+        "batched_over_plain": t_plain / t_batch, "rays_per_step": traced, "rays_nominal": rays,
+        "voxelize": {"seconds": t_vox, "instances": 10000, "source_voxels": src_voxels,
+                     "gvoxels_per_s": src_voxels / t_vox / 1e9},
+        "tuning": ctx.get_tuning(), "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="vxl", choices=["vxl", "reference"])
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c3"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--tuning", default="", help="tile_px,kstep,leap,order for the occlusion kernel")
+    ap.add_argument("--tuning", default="", help="tile_px,kstep,leap,order,tile_w,grab for the occlusion kernel")
+    ap.add_argument("--autotune", action="store_true", help="search the launch shape first and cache it")
     args = ap.parse_args()
+    if args.workload == "c3":
+        run_gpu_c3(args)
+        return
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         run_reference(args, wl)

@@ -304,8 +304,10 @@ def trace_rays(ctx: Context, grid: Grid, d_rays, n: int, mode: int, d_records, s
 
 
 def trace_occlusion(ctx: Context, grid: Grid, pos, nrm, rough, npix: int, params: TraceParams, shadow=None,
-                    ao=None, ao_vis=None, spec=None, spec_t=None, records=None, stream=None):
-    gb = GBuffer(_ptr(pos), _ptr(nrm), _ptr(rough), npix, 0, 0)
+                    ao=None, ao_vis=None, spec=None, spec_t=None, records=None, stream=None, width=0, height=0):
+    """width/height (optional, width*height == npix) let the kernel use
+    image-block tiles (vxl_tuning.tile_w)."""
+    gb = GBuffer(_ptr(pos), _ptr(nrm), _ptr(rough), npix, width, height)
     out = Outputs(_ptr(shadow), _ptr(ao), _ptr(ao_vis), _ptr(spec), _ptr(spec_t), _ptr(records))
     check(lib().vxl_trace_occlusion(ctx.handle, grid.handle, C.byref(gb), C.byref(params), C.byref(out),
                                     _stream(stream)))
