@@ -465,13 +465,106 @@ def run_gpu_c3(args):
     print(json.dumps(line))
 
 
+def run_gpu_c4(args):
+    """C4, the differentiable variant: 128^3 soft grid (opacity
+    sigmoid(8 (noise - 0.55)), albedo U[0,1)), 512x512 G-buffer of the matching
+    binary scene, 1 shadow + 16 AO rays per pixel of length 24; loss = MSE
+    against a target rendered with a second albedo seed. One step = forward,
+    dL/dimage, zeroing the gradient and the adjoint. Reports the forward and
+    adjoint times and their ratio; the CPU baseline is the FP64 oracle
+    (forward + adjoint) on a pixel sample."""
+    import torch
+
+    import voxelengine_gb300 as V
+    from voxelengine_gb300 import scenes as S
+
+    V.build()
+    ctx = V.Context(0)
+    n, W, H, seed = 128, 512, 512, 2024
+    P = V.make_soft_params(light_dir=S.light_dir(seed), bias=0.5, length=24.0, k_sun=0.7, k_amb=0.5, n_shadow=1,
+                           n_ao=16, seed=seed)
+    sc = S.make_soft_scene(ctx, n, W, H, seed, albedo_seed=1, params=P)
+    tg = S.make_soft_scene(ctx, n, W, H, seed, albedo_seed=2, params=P)
+    npix = sc["npix"]
+    img = torch.empty((npix, 3), dtype=torch.float32, device="cuda")
+    light = torch.empty_like(img)
+    target = torch.empty_like(img)
+    V.trace_soft_fwd(ctx, tg["soft"], tg["pos"], tg["nrm"], npix, P, target)
+    grad = torch.zeros_like(sc["soft"])
+    gi = torch.empty_like(img)
+    valid = int((sc["nrm3"].abs().sum(1) > 0).sum().item())
+    rays = valid * 17
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def fwd():
+        V.trace_soft_fwd(ctx, sc["soft"], sc["pos"], sc["nrm"], npix, P, img, light)
+
+    def bwd():
+        V.trace_soft_bwd(ctx, sc["soft"], sc["pos"], sc["nrm"], npix, P, gi, light, grad)
+
+    def step():
+        fwd()
+        torch.sub(img, target, out=gi)
+        gi.mul_(2.0 / img.numel())
+        grad.zero_()
+        bwd()
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            ts.append((a, b))
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in ts) / 1e3 / args.steps
+
+    step()
+    with ClockSampler(0) as clk:
+        t_fwd = timed(fwd)
+        t_bwd = timed(bwd)
+        t_step = timed(step)
+    loss = float(((img - target) ** 2).mean())
+    line = {
+        "metric": "Grays/s soft-opacity forward + adjoint (exact voxel DDA cells)",
+        "value": rays / t_step / 1e9, "unit": "Grays/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded soft grid and G-buffer)",
+        "config": {"workload": "soft-128^3-512x512-1shadow+16ao(L24)-mse", "l2": "flushed between timed steps"},
+        "forward_ms": t_fwd * 1e3, "adjoint_ms": t_bwd * 1e3, "adjoint_over_forward": t_bwd / t_fwd,
+        "rays_per_step": rays, "loss": loss, "gpu_launches": 2, "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        import oracle
+
+        vox = sc["soft"].cpu().numpy()
+        pos, nrm = sc["pos3"].cpu().numpy(), sc["nrm3"].cpu().numpy()
+        gih = gi.cpu().numpy()
+        op = oracle.make_soft_params(light_dir=list(P.light_dir), bias=P.bias, length=P.len, k_sun=P.k_sun,
+                                     k_amb=P.k_amb, n_shadow=P.n_shadow, n_ao=P.n_ao, seed=P.seed)
+        sel = np.arange(0, npix, 64)
+        live = int((np.abs(nrm[sel]).sum(1) > 0).sum())
+        threads = min(4, os.cpu_count() or 1)
+        t0 = time.perf_counter()
+        oracle.soft_render(vox, pos[sel], nrm[sel], op, gih[sel], threads=threads)
+        t = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": live * 17 / t / 1e9, "unit": "Grays/s", "cores": threads, "kind": "port",
+                                "sample": "FP64 oracle forward+adjoint on every 64th pixel (%d rays)" % (live * 17)}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="vxl", choices=["vxl", "reference"])
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c3"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c3", "c4"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -480,6 +573,9 @@ def main():
     args = ap.parse_args()
     if args.workload == "c3":
         run_gpu_c3(args)
+        return
+    if args.workload == "c4":
+        run_gpu_c4(args)
         return
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":

@@ -316,6 +316,48 @@ vxl_status vxl_vox_destroyed(vxl_ctx* ctx, vxl_grid* grid, const vxl_model* mode
 vxl_status vxl_voxelize_noalloc(const vxl_grid_desc* grid, const vxl_model* models, int nmodels,
                                 const vxl_instance* instances, int n, int32_t* d_aabb, void* stream);
 
+/* ------------------------------------------- differentiable soft variant
+ * No counterpart in the reference (its grid is binary). A soft grid is a
+ * device float4 per fine voxel (opacity, albedo r, g, b), x fastest, dims
+ * nx, ny, nz even. Each G-buffer pixel with a non-zero normal traces
+ * n_shadow (0 or 1) rays along light_dir and n_ao cosine-weighted AO rays
+ * (the directions vxl_trace_occlusion's DDA mode uses for AO samples), all
+ * from pos + bias * nrm. A ray walks exactly the cells the reference DDA
+ * (Light.frag:29-81) visits up to t = len on an empty grid, cells outside the
+ * data being empty, and stops early once its transmittance is below 2^-40.
+ * With a = clamp(opacity, 0, 1 - 2^-12):
+ *   shadow ray  T_sh = prod (1 - a_i)
+ *   AO ray k    T_k = prod (1 - a_i),  C_k = sum_i (prod_{l<i} (1 - a_l)) a_i albedo_i
+ *   light[c]  = k_sun T_sh + k_amb / n_ao * sum_k (T_k + C_k[c])
+ *   image[c]  = albedo_s[c] * light[c]
+ * where s = floor(pos - 0.5 nrm) is the surface voxel (no contribution when it
+ * lies outside the grid). */
+typedef struct vxl_soft_params {
+    float light_dir[3];
+    float bias;
+    float len;     /* maxt of every ray */
+    float k_sun;
+    float k_amb;
+    int32_t n_shadow; /* 0 or 1 */
+    int32_t n_ao;     /* n_shadow + n_ao in [1, 32] */
+    uint32_t seed;
+} vxl_soft_params;
+
+/* Forward: image and light are device float[npix][3]; light (optional, may be
+ * NULL) is what vxl_trace_soft_bwd needs for the albedo gradient of the
+ * surface voxel. Deterministic. */
+vxl_status vxl_trace_soft_fwd(vxl_ctx* ctx, const float* d_soft, int nx, int ny, int nz, const vxl_gbuffer* gbuf,
+                              const vxl_soft_params* p, float* d_image, float* d_light, void* stream);
+/* Adjoint: ACCUMULATES dL/d(opacity, albedo) into d_grad_soft (float4 per
+ * voxel, same layout as d_soft) given d_grad_image = dL/dimage and the light
+ * from the forward call on the same inputs. The rays are walked again (no
+ * per-ray state is kept between the calls); float atomics make the low bits
+ * of the sum order-dependent. The opacity clamp's derivative is 1 on the
+ * closed interval [0, 1 - 2^-12]. */
+vxl_status vxl_trace_soft_bwd(vxl_ctx* ctx, const float* d_soft, int nx, int ny, int nz, const vxl_gbuffer* gbuf,
+                              const vxl_soft_params* p, const float* d_grad_image, const float* d_light,
+                              float* d_grad_soft, void* stream);
+
 /* .v asset reader (VoxAsset::Serialize, VoxAsset.h:42-50): u32 sx,sy,sz then
  * sx*sy*sz bytes. Query with data == NULL to get the sizes, then read into a
  * host buffer of sx*sy*sz bytes. */
@@ -327,6 +369,13 @@ vxl_status vxl_read_v(const char* path, int32_t* sx, int32_t* sy, int32_t* sz, u
  * centre exceeds thresh, plus the slab y < ground_y */
 vxl_status vxl_scene_noise(vxl_ctx* ctx, vxl_grid* grid, uint32_t seed, float thresh, float freq, int ground_y,
                            void* stream);
+/* Soft grid (float4 per voxel, layout of vxl_trace_soft_fwd): opacity =
+ * sigmoid(sharpness * (noise - thresh)) with the noise of vxl_scene_noise
+ * (so opacity > 0.5 exactly where vxl_scene_noise sets a voxel, up to
+ * rounding at the threshold), opacity 1 in the slab y < ground_y; albedo
+ * r, g, b uniform in [0, 1) from a hash of (albedo_seed, voxel, channel). */
+vxl_status vxl_scene_soft(vxl_ctx* ctx, float* d_soft, int nx, int ny, int nz, uint32_t seed, float thresh,
+                          float sharpness, float freq, int ground_y, uint32_t albedo_seed, void* stream);
 /* OR into the grid: nboxes seeded axis-aligned boxes with edges in [smin, smax] */
 vxl_status vxl_scene_boxes(vxl_ctx* ctx, vxl_grid* grid, uint32_t seed, int nboxes, int smin, int smax, void* stream);
 /* primary-visibility G-buffer from a pinhole camera (entry-face DDA):

@@ -50,6 +50,21 @@ class Params(C.Structure):
     ]
 
 
+class SoftParams(C.Structure):
+    """Same layout as ``vxl_soft_params`` (include/vxl.h)."""
+
+    _fields_ = [
+        ("light_dir", C.c_float * 3),
+        ("bias", C.c_float),
+        ("len", C.c_float),
+        ("k_sun", C.c_float),
+        ("k_amb", C.c_float),
+        ("n_shadow", C.c_int32),
+        ("n_ao", C.c_int32),
+        ("seed", C.c_uint32),
+    ]
+
+
 def build(force: bool = False, opt: str = "-O2") -> str:
     """Compile the oracle shared library into oracle/_build/ (idempotent)."""
     src = os.path.join(_HERE, "vxl_oracle.cpp")
@@ -122,6 +137,8 @@ def lib():
                                            ip]
             L.vo_fnv1a64.restype = C.c_uint64
             L.vo_fnv1a64.argtypes = [C.c_char_p]
+            L.vo_soft_render.argtypes = [fp, C.c_int, C.c_int, C.c_int, fp, fp, C.c_int, C.POINTER(SoftParams),
+                                         vp, C.c_int64, C.c_double, vp, vp, C.c_int]
             _lib = L
     return _lib
 
@@ -367,6 +384,37 @@ def vox_destroyed(g, model, world):
 
 def fnv1a64(s: str) -> int:
     return lib().vo_fnv1a64(s.encode())
+
+
+def make_soft_params(light_dir=(0.3, 0.8, 0.5), bias=0.5, length=24.0, k_sun=0.7, k_amb=0.5, n_shadow=1,
+                     n_ao=4, seed=7) -> SoftParams:
+    p = SoftParams()
+    p.light_dir[:] = list(light_dir)
+    p.bias, p.len, p.k_sun, p.k_amb = bias, length, k_sun, k_amb
+    p.n_shadow, p.n_ao, p.seed = n_shadow, n_ao, seed
+    return p
+
+
+def soft_render(vox, pos, nrm, params: SoftParams, grad_image=None, perturb_voxel=-1, perturb_delta=0.0,
+                threads=None):
+    """FP64 soft-opacity render of a float4 grid vox[nz,ny,nx,4] (opacity, albedo rgb).
+
+    Returns image[npix,3] (float64), or (image, grad_vox[nz,ny,nx,4]) when
+    grad_image (float32 [npix,3]) is given."""
+    vox = np.ascontiguousarray(vox, np.float32)
+    nz, ny, nx, _ = vox.shape
+    pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+    nrm = np.ascontiguousarray(nrm, np.float32).reshape(-1, 3)
+    n = pos.shape[0]
+    img = np.zeros((n, 3), np.float64)
+    gv = None
+    gi = None
+    if grad_image is not None:
+        gi = np.ascontiguousarray(grad_image, np.float32).reshape(n, 3)
+        gv = np.zeros(vox.shape, np.float64)
+    lib().vo_soft_render(_f(vox), nx, ny, nz, _f(pos), _f(nrm), n, C.byref(params), _vp(gi), int(perturb_voxel),
+                         float(perturb_delta), _vp(img), _vp(gv), threads or threads_default())
+    return img if gv is None else (img, gv)
 
 
 # ------------------------------------------------- layout conversions (numpy)

@@ -116,7 +116,10 @@ void parallel_for(int n, int threads, F&& f) {
 // ---------------------------------------------------------------------------
 // raycastShadowVolume, Sources/Shaders/lib/Light.frag:29-81 (mip 0 only: the
 // outer `++i < 4` loop re-runs an identical pass, see vo_dda_literal).
-int dda(const Grid& G, V3 o, V3 d, float maxt, vo_rec* r) {
+// `occ(x, y, z)` is the occupancy test of the visited cell; sx,sy,sz are the
+// ShadowVox byte dims (fine dims / 2).
+template <class Occ>
+int dda_t(int gsx, int gsy, int gsz, V3 o, V3 d, float maxt, vo_rec* r, Occ&& occ) {
     vo_rec rec{0, 0, 0, 0.0f, 0, 0};
     if (!ray_domain_ok(o, d)) {
         rec.flags = VO_F_EXIT_BOUNDS;
@@ -130,7 +133,7 @@ int dda(const Grid& G, V3 o, V3 d, float maxt, vo_rec* r) {
                (float)cz + (ss.z * 0.5f + 0.5f));
     V3 tm = v3((nb.x - o.x) / d.x, (nb.y - o.y) / d.y, (nb.z - o.z) / d.z);
     // clamp(current_voxel, ivec3(0), ivec3(u_VolumeDimension/mipSize)*2+1)
-    const int ux = G.sx * 2 + 1, uy = G.sy * 2 + 1, uz = G.sz * 2 + 1;
+    const int ux = gsx * 2 + 1, uy = gsy * 2 + 1, uz = gsz * 2 + 1;
     int n = 0;
     float totalt = 0.0f;
     do {
@@ -147,7 +150,7 @@ int dda(const Grid& G, V3 o, V3 d, float maxt, vo_rec* r) {
             return 0;
         }
         rec.steps++;
-        bool voxel = G.volume_at(cx, cy, cz, 0);
+        bool voxel = occ(cx, cy, cz);
         float best_t = tm.x * selx + tm.y * sely;
         best_t = best_t + tm.z * selz;
         if (voxel) {
@@ -169,6 +172,10 @@ int dda(const Grid& G, V3 o, V3 d, float maxt, vo_rec* r) {
     rec.t = totalt;
     if (r) *r = rec;
     return 0;
+}
+
+int dda(const Grid& G, V3 o, V3 d, float maxt, vo_rec* r) {
+    return dda_t(G.sx, G.sy, G.sz, o, d, maxt, r, [&](int x, int y, int z) { return G.volume_at(x, y, z, 0); });
 }
 
 // Shared body of raycastShadowVolumeSparse / SuperSparse,
@@ -880,3 +887,175 @@ uint64_t vo_fnv1a64(const char* s) {
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Soft-opacity / albedo variant (this library's differentiable model; no
+// reference counterpart). Every ray visits the cells the reference DDA
+// (Light.frag:29-81) visits on an empty grid, up to maxt = len, and stops
+// early once its transmittance falls below 2^-40. Opacity is clamped to
+// [0, 1 - 2^-12]; the clamp's derivative is taken as 1 on the closed interval.
+//   shadow ray:   T_sh = prod (1 - a_i)
+//   AO ray k:     T_k  = prod (1 - a_i),  C_k = sum_i T_<i a_i rho_i  (rgb)
+//   image:        I = rho_s * (k_sun T_sh + k_amb / K sum_k (T_k + C_k))
+// rho_s is the albedo of the surface voxel floor(pos - 0.5 nrm). The adjoint
+// uses prefix and suffix products (no division).
+namespace {
+
+const double kSoftAmax = 1.0 - 1.0 / 4096.0;
+const double kSoftTmin = 1.0 / 1099511627776.0;  // 2^-40: a ray stops once its transmittance is below this
+
+struct SoftRay {
+    std::vector<int64_t> cells;  // voxel index, -1 for cells outside the data grid
+};
+
+void soft_pixel(const float* vox, int nx, int ny, int nz, const float* pos, const float* nrm, int i,
+                const vo_soft_params& p, const float* grad_image, int64_t pv, double pdelta, double* image,
+                double* gacc) {
+    V3 P = load3(pos + 3 * (size_t)i), N = load3(nrm + 3 * (size_t)i);
+    double* I = image + 3 * (size_t)i;
+    I[0] = I[1] = I[2] = 0.0;
+    if (N.x == 0.0f && N.y == 0.0f && N.z == 0.0f) return;
+    const int sxi = (int)std::floor(P.x - N.x * 0.5f), syi = (int)std::floor(P.y - N.y * 0.5f),
+              szi = (int)std::floor(P.z - N.z * 0.5f);
+    if (sxi < 0 || syi < 0 || szi < 0 || sxi >= nx || syi >= ny || szi >= nz) return;
+    const int64_t s = (int64_t)sxi + (int64_t)syi * nx + (int64_t)szi * nx * ny;
+    const double rs[3] = {vox[4 * s + 1], vox[4 * s + 2], vox[4 * s + 3]};
+    auto alpha_raw = [&](int64_t v) { return (double)vox[4 * v] + (v == pv ? pdelta : 0.0); };
+    auto alpha = [&](int64_t v) {
+        double a = alpha_raw(v);
+        return a < 0.0 ? 0.0 : (a > kSoftAmax ? kSoftAmax : a);
+    };
+    auto walk = [&](V3 o, V3 d, std::vector<int64_t>& cells) {
+        cells.clear();
+        dda_t(nx / 2, ny / 2, nz / 2, o, d, p.len, nullptr, [&](int x, int y, int z) {
+            bool in = x >= 0 && y >= 0 && z >= 0 && x < nx && y < ny && z < nz;
+            cells.push_back(in ? (int64_t)x + (int64_t)y * nx + (int64_t)z * nx * ny : -1);
+            return false;
+        });
+    };
+    V3 O = add(P, mul(N, p.bias));
+    V3 T, B;
+    tangent_frame(N, &T, &B);
+    const int K = p.n_ao;
+    std::vector<int64_t> cells;
+    std::vector<double> pre, suf, sufc;
+    // per ray: T and C (and the cells for the adjoint)
+    double Tsh = 1.0, Tsum = 0.0, Csum[3] = {0, 0, 0};
+    struct RayRes {
+        std::vector<int64_t> cells;
+        double T, C[3];
+    };
+    std::vector<RayRes> rays;
+    auto trace = [&](V3 d) {
+        RayRes rr;
+        walk(O, d, rr.cells);
+        double t = 1.0, c[3] = {0, 0, 0};
+        for (size_t j = 0; j < rr.cells.size(); j++) {
+            int64_t v = rr.cells[j];
+            if (v < 0) continue;
+            double a = alpha(v);
+            for (int ch = 0; ch < 3; ch++) c[ch] += t * a * (double)vox[4 * v + 1 + ch];
+            t *= 1.0 - a;
+            if (t < kSoftTmin) {  // the walk ends here: later cells are not visited
+                rr.cells.resize(j + 1);
+                break;
+            }
+        }
+        rr.T = t;
+        for (int ch = 0; ch < 3; ch++) rr.C[ch] = c[ch];
+        rays.push_back(rr);
+    };
+    if (p.n_shadow > 0) trace(load3(p.light_dir));
+    for (int k = 0; k < K; k++) {
+        float u1 = rand01(p.seed, (uint32_t)i, 64u + 2u * k);
+        float u2 = rand01(p.seed, (uint32_t)i, 65u + 2u * k);
+        trace(frame_dir(T, B, N, cosine_sample(u1, u2)));
+    }
+    int r0 = 0;
+    if (p.n_shadow > 0) {
+        Tsh = rays[0].T;
+        r0 = 1;
+    }
+    for (int k = 0; k < K; k++) {
+        Tsum += rays[r0 + k].T;
+        for (int ch = 0; ch < 3; ch++) Csum[ch] += rays[r0 + k].C[ch];
+    }
+    const double ks = p.n_shadow > 0 ? (double)p.k_sun : 0.0;
+    const double ka = K > 0 ? (double)p.k_amb / K : 0.0;
+    double L[3];
+    for (int ch = 0; ch < 3; ch++) {
+        L[ch] = ks * Tsh + ka * (Tsum + Csum[ch]);
+        I[ch] = rs[ch] * L[ch];
+    }
+    if (!grad_image || !gacc) return;
+    const double gI[3] = {grad_image[3 * (size_t)i], grad_image[3 * (size_t)i + 1], grad_image[3 * (size_t)i + 2]};
+    for (int ch = 0; ch < 3; ch++) gacc[4 * s + 1 + ch] += gI[ch] * L[ch];
+    auto dclamp = [&](int64_t v) {
+        double a = alpha_raw(v);
+        return (a >= 0.0 && a <= kSoftAmax) ? 1.0 : 0.0;
+    };
+    for (size_t r = 0; r < rays.size(); r++) {
+        const bool is_sh = p.n_shadow > 0 && r == 0;
+        double w[3];
+        for (int ch = 0; ch < 3; ch++) w[ch] = gI[ch] * rs[ch] * (is_sh ? ks : ka);
+        const std::vector<int64_t>& cs = rays[r].cells;
+        const size_t m = cs.size();
+        pre.assign(m + 1, 1.0);
+        for (size_t j = 0; j < m; j++) pre[j + 1] = pre[j] * (cs[j] < 0 ? 1.0 : 1.0 - alpha(cs[j]));
+        suf.assign(m + 1, 1.0);     // suf[j] = prod_{l >= j} (1 - a_l)
+        sufc.assign(3 * (m + 1), 0.0);  // sum_{l >= j} prod_{j <= q < l}(1 - a_q) a_l rho_l
+        for (size_t j = m; j-- > 0;) {
+            double a = cs[j] < 0 ? 0.0 : alpha(cs[j]);
+            suf[j] = suf[j + 1] * (1.0 - a);
+            for (int ch = 0; ch < 3; ch++) {
+                double rho = cs[j] < 0 ? 0.0 : (double)vox[4 * cs[j] + 1 + ch];
+                sufc[3 * j + ch] = a * rho + (1.0 - a) * sufc[3 * (j + 1) + ch];
+            }
+        }
+        for (size_t j = 0; j < m; j++) {
+            int64_t v = cs[j];
+            if (v < 0) continue;
+            double dT = -pre[j] * suf[j + 1];  // d T / d a_j
+            double ga = 0.0;
+            for (int ch = 0; ch < 3; ch++) {
+                double dC = 0.0;
+                if (!is_sh) {
+                    double rho = (double)vox[4 * v + 1 + ch];
+                    dC = pre[j] * rho - pre[j] * sufc[3 * (j + 1) + ch];
+                    gacc[4 * v + 1 + ch] += w[ch] * pre[j] * alpha(v);
+                }
+                ga += w[ch] * (dT + dC);
+            }
+            gacc[4 * v] += ga * dclamp(v);
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" void vo_soft_render(const float* vox, int nx, int ny, int nz, const float* pos, const float* nrm, int npix,
+                               const vo_soft_params* p, const float* grad_image, int64_t perturb_voxel,
+                               double perturb_delta, double* image, double* grad_vox, int threads) {
+    const size_t nv = (size_t)nx * ny * nz;
+    if (!grad_image || !grad_vox) {
+        parallel_for(npix, threads, [&](int i) {
+            soft_pixel(vox, nx, ny, nz, pos, nrm, i, *p, nullptr, perturb_voxel, perturb_delta, image, nullptr);
+        });
+        return;
+    }
+    int T = threads < 1 ? 1 : (threads > 4 ? 4 : threads);
+    std::vector<std::vector<double>> acc(T, std::vector<double>(4 * nv, 0.0));
+    std::vector<std::thread> ts;
+    for (int t = 0; t < T; t++)
+        ts.emplace_back([&, t]() {
+            for (int i = t; i < npix; i += T)
+                soft_pixel(vox, nx, ny, nz, pos, nrm, i, *p, grad_image, perturb_voxel, perturb_delta, image,
+                           acc[t].data());
+        });
+    for (auto& t : ts) t.join();
+    for (size_t k = 0; k < 4 * nv; k++) {
+        double s = 0.0;
+        for (int t = 0; t < T; t++) s += acc[t][k];
+        grad_vox[k] = s;
+    }
+}

@@ -125,6 +125,27 @@ void vo_vox_destroyed(uint8_t* g, int sx, int sy, int sz, const uint8_t* model, 
 
 uint64_t vo_fnv1a64(const char* s);
 
+/* Soft-opacity / albedo variant (no reference counterpart), FP64. Same layout
+ * as vxl_soft_params in include/vxl.h. */
+typedef struct vo_soft_params {
+    float light_dir[3];
+    float bias;
+    float len;
+    float k_sun;
+    float k_amb;
+    int32_t n_shadow;
+    int32_t n_ao;
+    uint32_t seed;
+} vo_soft_params;
+
+/* vox: float4 per voxel (opacity, albedo rgb), x fastest, nx,ny,nz even.
+ * image: double[npix*3]. grad_image (optional, float[npix*3]) = dL/dI; then
+ * grad_vox (double[nvox*4]) receives dL/d(opacity, albedo). perturb_voxel >= 0
+ * adds perturb_delta (in double) to that voxel's opacity (finite differences). */
+void vo_soft_render(const float* vox, int nx, int ny, int nz, const float* pos, const float* nrm, int npix,
+                    const vo_soft_params* p, const float* grad_image, int64_t perturb_voxel, double perturb_delta,
+                    double* image, double* grad_vox, int threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -20,6 +20,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libvxl.so")
 
 VXL_OK = 0
+VXL_ERR_INVALID_ARG, VXL_ERR_OOM, VXL_ERR_CUDA, VXL_ERR_TIMEOUT = 1, 2, 3, 4
+VXL_ERR_OUT_OF_RANGE, VXL_ERR_IO, VXL_ERR_NOT_SUPPORTED = 5, 6, 7
 MODE_DDA, MODE_SPARSE, MODE_SUPERSPARSE = 0, 1, 2
 OP_CLEAR, OP_SET = 0, 1
 RF_HIT, RF_SELX, RF_SELY, RF_SELZ = 1, 2, 4, 8
@@ -38,7 +40,8 @@ EXPORTED = [
     "vxl_batch_run", "vxl_batch_destroy", "vxl_batch_info", "vxl_light_ambient",
     "vxl_light_reflection", "vxl_light_point", "vxl_voxelize", "vxl_voxelize_noalloc", "vxl_shadowvox_update",
     "vxl_vox_destroyed",
-    "vxl_read_v", "vxl_scene_noise", "vxl_scene_boxes", "vxl_scene_gbuffer",
+    "vxl_trace_soft_fwd", "vxl_trace_soft_bwd",
+    "vxl_read_v", "vxl_scene_soft", "vxl_scene_noise", "vxl_scene_boxes", "vxl_scene_gbuffer",
 ]
 
 
@@ -81,6 +84,11 @@ class Tuning(C.Structure):
 
 class BatchItem(C.Structure):
     _fields_ = [("grid", C.c_void_p), ("gbuf", GBuffer), ("params", TraceParams), ("out", Outputs)]
+
+
+class SoftParams(C.Structure):
+    _fields_ = [("light_dir", C.c_float * 3), ("bias", C.c_float), ("len", C.c_float), ("k_sun", C.c_float),
+                ("k_amb", C.c_float), ("n_shadow", C.c_int32), ("n_ao", C.c_int32), ("seed", C.c_uint32)]
 
 
 class Model(C.Structure):
@@ -151,6 +159,11 @@ def lib():
         L.vxl_vox_destroyed.argtypes = [vp, vp, C.POINTER(Model), C.POINTER(f * 16), vp, vp]
         L.vxl_read_v.argtypes = [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), vp,
                                  C.c_size_t]
+        L.vxl_trace_soft_fwd.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.POINTER(GBuffer), C.POINTER(SoftParams),
+                                         vp, vp, vp]
+        L.vxl_trace_soft_bwd.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.POINTER(GBuffer), C.POINTER(SoftParams),
+                                         vp, vp, vp, vp]
+        L.vxl_scene_soft.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.c_uint32, f, f, f, C.c_int, C.c_uint32, vp]
         L.vxl_scene_noise.argtypes = [vp, vp, C.c_uint32, f, f, C.c_int, vp]
         L.vxl_scene_boxes.argtypes = [vp, vp, C.c_uint32, C.c_int, C.c_int, C.c_int, vp]
         L.vxl_scene_gbuffer.argtypes = [vp, vp, C.POINTER(f * 3), C.POINTER(f * 3), f, C.c_int, C.c_int, C.c_uint32,
@@ -381,6 +394,43 @@ def scene_gbuffer(ctx, grid, cam, target, W, H, seed, d_pos, d_nrm, d_rough, tan
     check(lib().vxl_scene_gbuffer(ctx.handle, grid.handle, C.byref(_f3(cam)), C.byref(_f3(target)),
                                   float(tan_half_fov), W, H, seed, _ptr(d_pos), _ptr(d_nrm), _ptr(d_rough),
                                   _stream(stream)))
+
+
+def make_soft_params(light_dir=(0.3, 0.8, 0.5), bias=0.5, length=24.0, k_sun=0.7, k_amb=0.5, n_shadow=1, n_ao=16,
+                     seed=7) -> SoftParams:
+    p = SoftParams()
+    p.light_dir[:] = [float(x) for x in light_dir]
+    p.bias, p.len, p.k_sun, p.k_amb = bias, length, k_sun, k_amb
+    p.n_shadow, p.n_ao, p.seed = n_shadow, n_ao, seed
+    return p
+
+
+def _soft_dims(soft):
+    nz, ny, nx, four = soft.shape
+    assert four == 4, "soft grid is [nz, ny, nx, 4]"
+    return nx, ny, nz
+
+
+def trace_soft_fwd(ctx, soft, pos, nrm, npix: int, params: SoftParams, image, light=None, stream=None):
+    """Soft-opacity forward (vxl_trace_soft_fwd); soft is a float32 [nz, ny, nx, 4] device tensor."""
+    nx, ny, nz = _soft_dims(soft)
+    gb = GBuffer(_ptr(pos), _ptr(nrm), None, npix, 0, 0)
+    check(lib().vxl_trace_soft_fwd(ctx.handle, _ptr(soft), nx, ny, nz, C.byref(gb), C.byref(params), _ptr(image),
+                                   _ptr(light), _stream(stream)))
+
+
+def trace_soft_bwd(ctx, soft, pos, nrm, npix: int, params: SoftParams, grad_image, light, grad_soft, stream=None):
+    """Adjoint (vxl_trace_soft_bwd): accumulates into grad_soft (same shape as soft)."""
+    nx, ny, nz = _soft_dims(soft)
+    gb = GBuffer(_ptr(pos), _ptr(nrm), None, npix, 0, 0)
+    check(lib().vxl_trace_soft_bwd(ctx.handle, _ptr(soft), nx, ny, nz, C.byref(gb), C.byref(params),
+                                   _ptr(grad_image), _ptr(light), _ptr(grad_soft), _stream(stream)))
+
+
+def scene_soft(ctx, soft, seed, thresh=0.55, sharpness=8.0, freq=1.0 / 32.0, ground_y=8, albedo_seed=1, stream=None):
+    nx, ny, nz = _soft_dims(soft)
+    check(lib().vxl_scene_soft(ctx.handle, _ptr(soft), nx, ny, nz, seed, thresh, sharpness, freq, ground_y,
+                               albedo_seed, _stream(stream)))
 
 
 def _models(models):

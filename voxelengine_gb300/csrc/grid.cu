@@ -158,6 +158,23 @@ __global__ void k_scene_noise(GridView g, uint64_t* words, uint32_t seed, float 
     if (out) words[w] |= out;
 }
 
+// soft grid: one thread per voxel, float4 (opacity, albedo rgb)
+__global__ void k_scene_soft(float4* soft, int nx, int ny, int nz, uint32_t seed, float thresh, float sharp,
+                             float freq, int ground_y, uint32_t aseed_h, uint32_t nvox) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nvox) return;
+    const int x = (int)(i % (uint32_t)nx), y = (int)((i / (uint32_t)nx) % (uint32_t)ny),
+              z = (int)(i / ((uint32_t)nx * (uint32_t)ny));
+    (void)nz;
+    float a = 1.0f;
+    if (y >= ground_y) {
+        const float v = noise_octaves((float)x + 0.5f, (float)y + 0.5f, (float)z + 0.5f, seed, freq, 3);
+        a = 1.0f / (1.0f + expf(-sharp * (v - thresh)));
+    }
+    const uint32_t h = pcg(aseed_h + i);
+    soft[i] = make_float4(a, u01(pcg(h)), u01(pcg(h + 1u)), u01(pcg(h + 2u)));
+}
+
 // box i: per axis size smin + pcg(base+2a) % (smax-smin+1) (clamped to the
 // grid), position pcg(base+2a+1) % (n-size+1); base = pcg(pcg(seed^0x5bd1e995)+i)
 __device__ __forceinline__ void box_params(uint32_t seed, int i, const int* n, int smin, int smax, int* b) {
@@ -326,6 +343,17 @@ vxl_status launch_scene_noise(vxl_grid* g, uint32_t seed, float thresh, float fr
     g->ctx->launches++;
     VXL_TRY_CUDA(cudaGetLastError());
     return launch_build_tile_mask(g, s);
+}
+
+vxl_status launch_scene_soft(vxl_ctx* ctx, float* soft, int nx, int ny, int nz, uint32_t seed, float thresh,
+                             float sharpness, float freq, int ground_y, uint32_t albedo_seed, cudaStream_t s) {
+    const size_t n = (size_t)nx * ny * nz;
+    if (n == 0) return VXL_OK;
+    k_scene_soft<<<blocks_for(n, 256), 256, 0, s>>>(reinterpret_cast<float4*>(soft), nx, ny, nz, seed, thresh,
+                                                   sharpness, freq, ground_y, pcg(albedo_seed), (uint32_t)n);
+    ctx->launches++;
+    VXL_TRY_CUDA(cudaGetLastError());
+    return VXL_OK;
 }
 
 vxl_status launch_scene_boxes(vxl_grid* g, uint32_t seed, int nboxes, int smin, int smax, cudaStream_t s) {

@@ -2,6 +2,7 @@
 // Validates arguments, owns contexts and grids, plans voxelizer runs, and
 // dispatches to the kernel launchers. Compiled without FMA contraction so the
 // host-side matrix arithmetic (glm::translate) matches the reference bit for bit.
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -697,6 +698,64 @@ vxl_status vxl_scene_noise(vxl_ctx* ctx, vxl_grid* g, uint32_t seed, float thres
     if (!ctx || !grid_ok(g)) return fail(VXL_ERR_INVALID_ARG, "scene_noise: bad argument");
     VXL_TRY(set_device(ctx));
     return launch_scene_noise(g, seed, thresh, freq, ground_y, (cudaStream_t)stream);
+}
+
+// soft grid dims: even (the walk's upper bound is dims + 1, as for the bit
+// grid), voxel indices fit an int32
+static vxl_status check_soft_grid(const float* soft, int nx, int ny, int nz, const char* who) {
+    if (!soft) return fail(VXL_ERR_INVALID_ARG, "%s: NULL soft grid", who);
+    if (((uintptr_t)soft & 15u) != 0) return fail(VXL_ERR_INVALID_ARG, "%s: soft grid not 16-byte aligned", who);
+    if (nx < 2 || ny < 2 || nz < 2 || (nx & 1) || (ny & 1) || (nz & 1))
+        return fail(VXL_ERR_INVALID_ARG, "%s: dims must be even and >= 2", who);
+    if ((int64_t)nx * ny * nz > (int64_t)INT32_MAX || nx > 32760 || ny > 32760 || nz > 32760)
+        return fail(VXL_ERR_OUT_OF_RANGE, "%s: soft grid too large", who);
+    return VXL_OK;
+}
+
+static vxl_status check_soft_call(const vxl_gbuffer* gb, const vxl_soft_params* p, const char* who) {
+    if (!gb || !p) return fail(VXL_ERR_INVALID_ARG, "%s: NULL argument", who);
+    if (gb->npix < 0 || gb->npix > (int64_t)INT32_MAX - 32) return fail(VXL_ERR_INVALID_ARG, "%s: bad npix", who);
+    if (gb->npix > 0 && (!gb->pos || !gb->nrm)) return fail(VXL_ERR_INVALID_ARG, "%s: NULL G-buffer", who);
+    if (p->n_shadow < 0 || p->n_shadow > 1 || p->n_ao < 0 || p->n_shadow + p->n_ao < 1 ||
+        p->n_shadow + p->n_ao > 32)
+        return fail(VXL_ERR_INVALID_ARG, "%s: need n_shadow in {0,1} and 1 <= n_shadow + n_ao <= 32", who);
+    if (!(p->len >= 0.0f) || !std::isfinite(p->len) || !std::isfinite(p->bias))
+        return fail(VXL_ERR_INVALID_ARG, "%s: len and bias must be finite, len >= 0", who);
+    return VXL_OK;
+}
+
+vxl_status vxl_trace_soft_fwd(vxl_ctx* ctx, const float* d_soft, int nx, int ny, int nz, const vxl_gbuffer* gb,
+                              const vxl_soft_params* p, float* d_image, float* d_light, void* stream) {
+    if (!ctx) return fail(VXL_ERR_INVALID_ARG, "trace_soft_fwd: NULL context");
+    VXL_TRY(check_soft_grid(d_soft, nx, ny, nz, "trace_soft_fwd"));
+    VXL_TRY(check_soft_call(gb, p, "trace_soft_fwd"));
+    if (gb->npix > 0 && !d_image) return fail(VXL_ERR_INVALID_ARG, "trace_soft_fwd: NULL image");
+    VXL_TRY(set_device(ctx));
+    return launch_soft_fwd(ctx, d_soft, nx, ny, nz, gb, p, d_image, d_light, (cudaStream_t)stream);
+}
+
+vxl_status vxl_trace_soft_bwd(vxl_ctx* ctx, const float* d_soft, int nx, int ny, int nz, const vxl_gbuffer* gb,
+                              const vxl_soft_params* p, const float* d_grad_image, const float* d_light,
+                              float* d_grad_soft, void* stream) {
+    if (!ctx) return fail(VXL_ERR_INVALID_ARG, "trace_soft_bwd: NULL context");
+    VXL_TRY(check_soft_grid(d_soft, nx, ny, nz, "trace_soft_bwd"));
+    VXL_TRY(check_soft_call(gb, p, "trace_soft_bwd"));
+    if (gb->npix > 0 && (!d_grad_image || !d_light || !d_grad_soft))
+        return fail(VXL_ERR_INVALID_ARG, "trace_soft_bwd: NULL grad_image, light or grad_soft");
+    if (((uintptr_t)d_grad_soft & 15u) != 0)
+        return fail(VXL_ERR_INVALID_ARG, "trace_soft_bwd: grad_soft not 16-byte aligned");
+    VXL_TRY(set_device(ctx));
+    return launch_soft_bwd(ctx, d_soft, nx, ny, nz, gb, p, d_grad_image, d_light, d_grad_soft,
+                           (cudaStream_t)stream);
+}
+
+vxl_status vxl_scene_soft(vxl_ctx* ctx, float* d_soft, int nx, int ny, int nz, uint32_t seed, float thresh,
+                          float sharpness, float freq, int ground_y, uint32_t albedo_seed, void* stream) {
+    if (!ctx) return fail(VXL_ERR_INVALID_ARG, "scene_soft: NULL context");
+    VXL_TRY(check_soft_grid(d_soft, nx, ny, nz, "scene_soft"));
+    VXL_TRY(set_device(ctx));
+    return launch_scene_soft(ctx, d_soft, nx, ny, nz, seed, thresh, sharpness, freq, ground_y, albedo_seed,
+                             (cudaStream_t)stream);
 }
 
 vxl_status vxl_scene_boxes(vxl_ctx* ctx, vxl_grid* g, uint32_t seed, int nboxes, int smin, int smax, void* stream) {

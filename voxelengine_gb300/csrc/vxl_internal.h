@@ -77,6 +77,13 @@ vxl_status launch_build_tile_mask(vxl_grid* g, cudaStream_t s);
 vxl_status launch_grid_count(const vxl_grid* g, unsigned long long* d_out, cudaStream_t s);
 vxl_status launch_scene_noise(vxl_grid* g, uint32_t seed, float thresh, float freq, int ground_y, cudaStream_t s);
 vxl_status launch_scene_boxes(vxl_grid* g, uint32_t seed, int nboxes, int smin, int smax, cudaStream_t s);
+vxl_status launch_scene_soft(vxl_ctx* ctx, float* soft, int nx, int ny, int nz, uint32_t seed, float thresh,
+                             float sharpness, float freq, int ground_y, uint32_t albedo_seed, cudaStream_t s);
+vxl_status launch_soft_fwd(vxl_ctx* ctx, const float* soft, int nx, int ny, int nz, const vxl_gbuffer* gb,
+                           const vxl_soft_params* p, float* image, float* light, cudaStream_t st);
+vxl_status launch_soft_bwd(vxl_ctx* ctx, const float* soft, int nx, int ny, int nz, const vxl_gbuffer* gb,
+                           const vxl_soft_params* p, const float* grad_image, const float* light, float* grad_soft,
+                           cudaStream_t st);
 vxl_status launch_scene_gbuffer(const vxl_grid* g, const float cam[3], const float target[3], float tan_half_fov,
                                 int W, int H, uint32_t seed, float* pos, float* nrm, float* rough, cudaStream_t s);
 

@@ -94,6 +94,21 @@ def make_scene(ctx, n, W, H, seed, thresh=0.55, boxes=0, params=None, device_ten
                 cam=cam, seed=seed)
 
 
+def make_soft_scene(ctx, n, W, H, seed, albedo_seed=1, thresh=0.55, sharpness=8.0, params=None):
+    """Differentiable workload: soft grid [n,n,n,4] with opacity
+    sigmoid(sharpness * (noise - thresh)) and uniform albedo, plus the G-buffer
+    of the matching binary scene (the voxels with opacity > 0.5)."""
+    import torch
+
+    sc = make_scene(ctx, n, W, H, seed, thresh=thresh)
+    soft = torch.empty((n, n, n, 4), dtype=torch.float32, device="cuda")
+    V.scene_soft(ctx, soft, seed, thresh, sharpness, 1.0 / 32.0, 8, albedo_seed)
+    P = params or V.make_soft_params(light_dir=light_dir(seed), bias=0.5, length=24.0, k_sun=0.7, k_amb=0.5,
+                                     n_shadow=1, n_ao=16, seed=seed)
+    sc.update(soft=soft, soft_params=P, pos3=sc["pos"].view(-1, 3), nrm3=sc["nrm"].view(-1, 3))
+    return sc
+
+
 def batch_set(ctx, count=64, seed=7, edge_range=(64, 512), rays_range=(64 * 1024, 2 * 1024 * 1024),
               thresh_range=(0.45, 0.65), rays_per_pixel=10):
     """The uneven scene mix: edges log-uniform in edge_range (even), noise
