@@ -125,7 +125,7 @@ def test_soft_autograd_mse(vxl, ctx):
     torch.cuda.synchronize()
     g1, g2 = soft.grad.cpu().numpy(), grad.cpu().numpy()
     assert np.abs(g1 - g2).max() <= 1e-5 * np.abs(g2).max()
-    assert float(loss) > 0 and np.abs(g2).max() > 0
+    assert float(loss.detach()) > 0 and np.abs(g2).max() > 0
 
 
 def test_soft_binary_opacity_is_the_dda_shadow(vxl, ctx):
