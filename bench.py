@@ -35,6 +35,9 @@ WORKLOADS = {
                shadow_len=100.0, seed=2024),
     "c1": dict(n=256, W=640, H=360, boxes=0, n_shadow=1, n_ao=4, ao_len=16.0, n_spec=0, spec_len=256.0,
                shadow_len=100.0, seed=2024),
+    # stress: 2048^3 terrain (amplitude 512) + 50,000 instances of edge 16-128, 4K frame
+    "c5": dict(kind="terrain", n=2048, W=3840, H=2160, boxes=0, instances=50000, n_shadow=1, n_ao=16, ao_len=64.0,
+               n_spec=1, spec_len=256.0, shadow_len=256.0, seed=5),
 }
 L2_BYTES = 129 * 1024 * 1024
 
@@ -190,6 +193,10 @@ def run_reference(args, wl):
     rank, world, local, dist = dist_setup(args)
     if rank != 0:
         return
+    if wl.get("kind") == "terrain":
+        print(json.dumps({"impl": "reference", "unavailable": "stress scene: voxelizing 50,000 instances on the "
+                                                             "host cores exceeds the bounded reference run"}))
+        return
     n, W, H = wl["n"], wl["W"], wl["H"]
     threads = os.cpu_count() or 1
     g = oracle.scene_noise(n, n, n, seed=wl["seed"], threads=threads)
@@ -226,11 +233,19 @@ def run_reference(args, wl):
 
 
 def config_dict(wl):
-    return {"workload": "plain-%d^3-%dx%d-%dshadow+%dao(L%g)+%dspec" % (
-        wl["n"], wl["W"], wl["H"], wl["n_shadow"], wl["n_ao"], wl["ao_len"], wl["n_spec"]),
-        "grid": [wl["n"]] * 3, "image": [wl["W"], wl["H"]], "boxes": wl["boxes"],
-        "rays_per_pixel": wl["n_shadow"] + wl["n_ao"] + wl["n_spec"], "noise_threshold": 0.55,
+    terrain = wl.get("kind") == "terrain"
+    d = {"workload": "%s-%d^3-%dx%d-%dshadow+%dao(L%g)+%dspec" % (
+        "terrain" if terrain else "plain", wl["n"], wl["W"], wl["H"], wl["n_shadow"], wl["n_ao"], wl["ao_len"],
+        wl["n_spec"]),
+        "grid": [wl["n"]] * 3, "image": [wl["W"], wl["H"]],
+        "rays_per_pixel": wl["n_shadow"] + wl["n_ao"] + wl["n_spec"],
         "l2": "flushed between timed steps (256 MiB write outside the per-step events)"}
+    if terrain:
+        d.update(terrain={"base": wl["n"] / 16.0, "amplitude": 512.0, "octaves": 6}, instances=wl["instances"],
+                 instance_edges=[16, 128])
+    else:
+        d.update(boxes=wl["boxes"], noise_threshold=0.55)
+    return d
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -251,18 +266,30 @@ def run_gpu(args, wl):
     n, W, H = wl["n"], wl["W"], wl["H"]
     npix = W * H
     R = wl["n_shadow"] + wl["n_ao"] + wl["n_spec"]
-    G = V.Grid(ctx, n, n, n)
-    G.scene_noise(wl["seed"], 0.55, 1.0 / 32.0, 8)
-    if wl["boxes"]:
-        G.scene_boxes(wl["seed"], wl["boxes"], 4, 48)
-    cam, tgt = camera(n)
-    pos = torch.empty(npix * 3, dtype=torch.float32, device="cuda")
-    nrm = torch.empty_like(pos)
-    rough = torch.empty(npix, dtype=torch.float32, device="cuda")
-    V.scene_gbuffer(ctx, G, cam, tgt, W, H, wl["seed"], pos, nrm, rough)
-    P = V.make_params(light_dir=light_dir(wl["seed"]), cam_pos=cam, bias=0.5, shadow_len=wl["shadow_len"],
-                      ao_len=wl["ao_len"], spec_len=wl["spec_len"], n_shadow=wl["n_shadow"], n_ao=wl["n_ao"],
-                      n_spec=wl["n_spec"], seed=wl["seed"])
+    P_kw = dict(light_dir=light_dir(wl["seed"]), bias=0.5, shadow_len=wl["shadow_len"], ao_len=wl["ao_len"],
+                spec_len=wl["spec_len"], n_shadow=wl["n_shadow"], n_ao=wl["n_ao"], n_spec=wl["n_spec"],
+                seed=wl["seed"])
+    scene_extra = {}
+    if wl.get("kind") == "terrain":
+        from voxelengine_gb300 import scenes as S
+
+        sc = S.make_terrain_scene(ctx, n, W, H, seed=wl["seed"], n_instances=wl["instances"])
+        G, pos, nrm, rough, cam = sc["grid"], sc["pos"], sc["nrm"], sc["rough"], sc["cam"]
+        P = V.make_params(cam_pos=cam, **P_kw)
+        scene_extra["voxelize"] = {"seconds": sc["voxelize_seconds"], "instances": wl["instances"],
+                                   "source_voxels": sc["source_voxels"],
+                                   "gvoxels_per_s": sc["source_voxels"] / sc["voxelize_seconds"] / 1e9}
+    else:
+        G = V.Grid(ctx, n, n, n)
+        G.scene_noise(wl["seed"], 0.55, 1.0 / 32.0, 8)
+        if wl["boxes"]:
+            G.scene_boxes(wl["seed"], wl["boxes"], 4, 48)
+        cam, tgt = camera(n)
+        pos = torch.empty(npix * 3, dtype=torch.float32, device="cuda")
+        nrm = torch.empty_like(pos)
+        rough = torch.empty(npix, dtype=torch.float32, device="cuda")
+        V.scene_gbuffer(ctx, G, cam, tgt, W, H, wl["seed"], pos, nrm, rough)
+        P = V.make_params(cam_pos=cam, **P_kw)
     outs = {k: torch.empty(npix, dtype=torch.float32, device="cuda") for k in ("shadow", "ao", "ao_vis", "spec", "spec_t")}
     valid = int((nrm.view(-1, 3).abs().sum(1) > 0).sum().item())
     rays_per_step = valid * R
@@ -355,6 +382,7 @@ def run_gpu(args, wl):
         "tuning": ctx.get_tuning(),
         "clocks": clk.summary(),
     }
+    line.update(scene_extra)
     if not args.no_cpu_baseline:
         g8 = torch.zeros((n // 2) ** 3, dtype=torch.uint8, device="cuda")
         G.export_r8(g8)
@@ -362,9 +390,7 @@ def run_gpu(args, wl):
         g_np = g8.cpu().numpy().reshape(n // 2, n // 2, n // 2)
         import oracle
 
-        OP = oracle.make_params(light_dir=light_dir(wl["seed"]), cam_pos=cam, bias=0.5, shadow_len=wl["shadow_len"],
-                                ao_len=wl["ao_len"], spec_len=wl["spec_len"], n_shadow=wl["n_shadow"],
-                                n_ao=wl["n_ao"], n_spec=wl["n_spec"], seed=wl["seed"])
+        OP = oracle.make_params(cam_pos=cam, **P_kw)
         v, rows, dt, th = cpu_sample_rays_per_s(g_np, pos.cpu().numpy(), nrm.cpu().numpy(), rough.cpu().numpy(), OP,
                                                 W, H, budget_s=args.cpu_seconds)
         line["cpu_baseline"] = {"value": v / 1e9, "unit": "Grays/s", "cores": th, "kind": "port",

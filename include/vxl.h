@@ -376,6 +376,12 @@ vxl_status vxl_scene_noise(vxl_ctx* ctx, vxl_grid* grid, uint32_t seed, float th
  * r, g, b uniform in [0, 1) from a hash of (albedo_seed, voxel, channel). */
 vxl_status vxl_scene_soft(vxl_ctx* ctx, float* d_soft, int nx, int ny, int nz, uint32_t seed, float thresh,
                           float sharpness, float freq, int ground_y, uint32_t albedo_seed, void* stream);
+/* OR into the grid: heightfield terrain, voxel (x, y, z) set where
+ * (float)y < h(x, z) = base + amplitude * fbm(x + 0.5, 0.5, z + 0.5), fbm the
+ * octave noise of vxl_scene_noise with `octaves` octaves at frequency freq
+ * (values in [0, 1]). d_height (optional, device float[nz][nx]) receives h. */
+vxl_status vxl_scene_terrain(vxl_ctx* ctx, vxl_grid* grid, uint32_t seed, float base, float amplitude, float freq,
+                             int octaves, float* d_height, void* stream);
 /* OR into the grid: nboxes seeded axis-aligned boxes with edges in [smin, smax] */
 vxl_status vxl_scene_boxes(vxl_ctx* ctx, vxl_grid* grid, uint32_t seed, int nboxes, int smin, int smax, void* stream);
 /* primary-visibility G-buffer from a pinhole camera (entry-face DDA):

@@ -123,6 +123,8 @@ def lib():
             L.vo_value_noise3.argtypes = [C.c_float, C.c_float, C.c_float, C.c_uint32]
             L.vo_noise_octaves.restype = C.c_float
             L.vo_noise_octaves.argtypes = [C.c_float, C.c_float, C.c_float, C.c_uint32, C.c_float, C.c_int]
+            L.vo_scene_terrain.argtypes = [u8p, C.c_int, C.c_int, C.c_int, C.c_uint32, C.c_float, C.c_float,
+                                           C.c_float, C.c_int, vp, C.c_int]
             L.vo_scene_boxes.argtypes = [u8p, C.c_int, C.c_int, C.c_int, C.c_uint32, C.c_int, C.c_int, C.c_int]
             L.vo_box_params.argtypes = [C.c_uint32, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, ip]
             L.vo_gbuffer.argtypes = [u8p, C.c_int, C.c_int, C.c_int, fp, fp, C.c_float, C.c_int, C.c_int,
@@ -260,6 +262,30 @@ def occlusion(g, pos, nrm, rough, params: Params, with_recs=False, p0=0, p1=-1, 
     return out
 
 
+def occlusion_range(g, pos, nrm, rough, params: Params, p0, p1, threads=None):
+    """occlusion() for pixels [p0, p1) only, with records; outputs and records
+    are returned for that range alone (the pixel index, which seeds the ray
+    generator, stays the global one)."""
+    g, sx, sy, sz = _grid(g)
+    pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+    nrm = np.ascontiguousarray(nrm, np.float32).reshape(-1, 3)
+    rough = None if rough is None else np.ascontiguousarray(rough, np.float32).reshape(-1)
+    m = p1 - p0
+    R = params.n_shadow + params.n_ao + params.n_spec
+    out = {k: np.zeros(m, np.float32) for k in ("shadow", "ao", "ao_vis", "spec", "spec_t")}
+    recs = np.zeros(m * R, REC_DTYPE)
+
+    def shifted(a, per):  # address of element -p0*per, so that index p0 lands on a[0]
+        return C.c_void_p(a.ctypes.data - p0 * per * a.itemsize)
+
+    lib().vo_occlusion(_u8(g), sx, sy, sz, _f(pos), _f(nrm), _vp(rough), pos.shape[0], C.byref(params),
+                       shifted(out["shadow"], 1), shifted(out["ao"], 1), shifted(out["ao_vis"], 1),
+                       shifted(out["spec"], 1), shifted(out["spec_t"], 1), shifted(recs, R), p0, p1,
+                       threads or threads_default())
+    out["recs"] = recs
+    return out
+
+
 def light_ambient(g, wcp, nrm, depth, noise, threads=None):
     g, sx, sy, sz = _grid(g)
     wcp = np.ascontiguousarray(wcp, np.float32).reshape(-1, 3)
@@ -311,6 +337,17 @@ def scene_noise(nx, ny, nz, seed, thresh=0.55, freq=1.0 / 32.0, ground_y=8, thre
     lib().vo_scene_noise(_u8(g), sx, sy, sz, seed, C.c_float(thresh), C.c_float(freq), ground_y,
                          threads or threads_default())
     return g
+
+
+def scene_terrain(g, seed, base, amplitude, freq, octaves=5, threads=None):
+    """OR the heightfield terrain into an R8 grid (uint8[nz/2, ny/2, nx/2]);
+    returns the column heights float32[nz, nx]."""
+    sz, sy, sx = g.shape
+    assert g.flags.c_contiguous and g.dtype == np.uint8
+    h = np.zeros((2 * sz, 2 * sx), np.float32)
+    lib().vo_scene_terrain(_u8(g), sx, sy, sz, seed, C.c_float(base), C.c_float(amplitude), C.c_float(freq), octaves,
+                           _vp(h), threads or threads_default())
+    return h
 
 
 def scene_boxes(g, seed, nboxes, smin=4, smax=48):

@@ -741,6 +741,33 @@ void vo_scene_noise(uint8_t* g, int sx, int sy, int sz, uint32_t seed, float thr
     });
 }
 
+// heightfield terrain (this library's synthetic scene; no reference counterpart):
+// voxel (x, y, z) set where (float)y < base + amp * fbm(x + 0.5, 0.5, z + 0.5)
+void vo_scene_terrain(uint8_t* g, int sx, int sy, int sz, uint32_t seed, float base, float amp, float freq,
+                      int octaves, float* height, int threads) {
+    const int nx = 2 * sx, ny = 2 * sy, nz = 2 * sz;
+    std::vector<float> hv;
+    if (!height) {
+        hv.resize((size_t)nx * nz);
+        height = hv.data();
+    }
+    parallel_for(nz, threads, [&](int z) {
+        for (int x = 0; x < nx; x++) {
+            const float v = noise_octaves((float)x + 0.5f, 0.5f, (float)z + 0.5f, seed, freq, octaves);
+            const float m = amp * v;
+            height[(size_t)z * nx + x] = base + m;
+        }
+    });
+    // one task per byte-plane pair of z so that tasks write disjoint bytes
+    parallel_for(sz, threads, [&](int bz) {
+        for (int z = 2 * bz; z < 2 * bz + 2; z++)
+            for (int x = 0; x < nx; x++) {
+                const float h = height[(size_t)z * nx + x];
+                for (int y = 0; y < ny && (float)y < h; y++) set_fine(g, sx, sy, x, y, z);
+            }
+    });
+}
+
 void vo_box_params(uint32_t seed, int i, int nx, int ny, int nz, int smin, int smax, int* out6) {
     uint32_t base = pcg(pcg(seed ^ 0x5bd1e995u) + (uint32_t)i);
     int n[3] = {nx, ny, nz};

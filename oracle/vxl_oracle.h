@@ -104,6 +104,8 @@ void vo_scene_noise(uint8_t* g, int sx, int sy, int sz, uint32_t seed, float thr
                     int ground_y, int threads);
 float vo_value_noise3(float x, float y, float z, uint32_t seed);
 float vo_noise_octaves(float x, float y, float z, uint32_t seed, float freq, int octaves);
+void vo_scene_terrain(uint8_t* g, int sx, int sy, int sz, uint32_t seed, float base, float amp, float freq,
+                      int octaves, float* height, int threads);
 void vo_scene_boxes(uint8_t* g, int sx, int sy, int sz, uint32_t seed, int nboxes, int smin, int smax);
 void vo_box_params(uint32_t seed, int i, int nx, int ny, int nz, int smin, int smax, int* out6);
 

@@ -41,7 +41,7 @@ EXPORTED = [
     "vxl_light_reflection", "vxl_light_point", "vxl_voxelize", "vxl_voxelize_noalloc", "vxl_shadowvox_update",
     "vxl_vox_destroyed",
     "vxl_trace_soft_fwd", "vxl_trace_soft_bwd",
-    "vxl_read_v", "vxl_scene_soft", "vxl_scene_noise", "vxl_scene_boxes", "vxl_scene_gbuffer",
+    "vxl_read_v", "vxl_scene_soft", "vxl_scene_terrain", "vxl_scene_noise", "vxl_scene_boxes", "vxl_scene_gbuffer",
 ]
 
 
@@ -165,6 +165,7 @@ def lib():
                                          vp, vp, vp, vp]
         L.vxl_scene_soft.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.c_uint32, f, f, f, C.c_int, C.c_uint32, vp]
         L.vxl_scene_noise.argtypes = [vp, vp, C.c_uint32, f, f, C.c_int, vp]
+        L.vxl_scene_terrain.argtypes = [vp, vp, C.c_uint32, f, f, f, C.c_int, vp, vp]
         L.vxl_scene_boxes.argtypes = [vp, vp, C.c_uint32, C.c_int, C.c_int, C.c_int, vp]
         L.vxl_scene_gbuffer.argtypes = [vp, vp, C.POINTER(f * 3), C.POINTER(f * 3), f, C.c_int, C.c_int, C.c_uint32,
                                         vp, vp, vp, vp]
@@ -284,6 +285,10 @@ class Grid:
 
     def scene_noise(self, seed, thresh=0.55, freq=1.0 / 32.0, ground_y=8, stream=None):
         check(lib().vxl_scene_noise(self.ctx.handle, self._h, seed, thresh, freq, ground_y, _stream(stream)))
+
+    def scene_terrain(self, seed, base, amplitude, freq, octaves=5, d_height=None, stream=None):
+        check(lib().vxl_scene_terrain(self.ctx.handle, self._h, seed, base, amplitude, freq, octaves, _ptr(d_height),
+                                      _stream(stream)))
 
     def scene_boxes(self, seed, nboxes, smin=4, smax=48, stream=None):
         check(lib().vxl_scene_boxes(self.ctx.handle, self._h, seed, nboxes, smin, smax, _stream(stream)))

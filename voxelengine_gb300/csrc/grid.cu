@@ -158,6 +158,35 @@ __global__ void k_scene_noise(GridView g, uint64_t* words, uint32_t seed, float 
     if (out) words[w] |= out;
 }
 
+// heightfield terrain: column height base + amp * fbm(x + 0.5, 0.5, z + 0.5)
+__global__ void k_heightmap(float* h, int nx, int nz, uint32_t seed, float base, float amp, float freq, int octaves) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (uint32_t)nx * (uint32_t)nz) return;
+    const int x = (int)(i % (uint32_t)nx), z = (int)(i / (uint32_t)nx);
+    const float v = noise_octaves((float)x + 0.5f, 0.5f, (float)z + 0.5f, seed, freq, octaves);
+    h[i] = base + amp * v;
+}
+// one thread per word; voxel (x, y, z) is solid when (float)y < h(x, z)
+__global__ void k_scene_terrain(GridView g, uint64_t* words, const float* __restrict__ h, uint32_t nwords) {
+    const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nwords) return;
+    int x0, y0, z0;
+    word_origin(g, w, &x0, &y0, &z0);
+    if (x0 >= g.nx || y0 >= g.ny || z0 >= g.nz) return;
+    uint64_t out = 0;
+    for (int lz = 0; lz < 4; lz++)
+        for (int lx = 0; lx < 4; lx++) {
+            const int x = x0 + lx, z = z0 + lz;
+            if (x >= g.nx || z >= g.nz) continue;
+            const float hh = h[(size_t)z * g.nx + x];
+            for (int ly = 0; ly < 4; ly++) {
+                const int y = y0 + ly;
+                if (y < g.ny && (float)y < hh) out |= 1ull << (lx | (ly << 2) | (lz << 4));
+            }
+        }
+    if (out) words[w] |= out;
+}
+
 // soft grid: one thread per voxel, float4 (opacity, albedo rgb)
 __global__ void k_scene_soft(float4* soft, int nx, int ny, int nz, uint32_t seed, float thresh, float sharp,
                              float freq, int ground_y, uint32_t aseed_h, uint32_t nvox) {
@@ -354,6 +383,23 @@ vxl_status launch_scene_soft(vxl_ctx* ctx, float* soft, int nx, int ny, int nz, 
     ctx->launches++;
     VXL_TRY_CUDA(cudaGetLastError());
     return VXL_OK;
+}
+
+vxl_status launch_scene_terrain(vxl_grid* g, uint32_t seed, float base, float amp, float freq, int octaves,
+                                float* d_height, cudaStream_t s) {
+    const size_t ncol = (size_t)g->nx * g->nz;
+    float* h = d_height;
+    if (!h) {
+        void* p;
+        VXL_TRY(ctx_scratch(g->ctx, ncol * sizeof(float), &p));
+        h = (float*)p;
+    }
+    k_heightmap<<<blocks_for(ncol, 256), 256, 0, s>>>(h, g->nx, g->nz, seed, base, amp, freq, octaves);
+    GridView v = view_of(g);
+    k_scene_terrain<<<blocks_for(g->nwords, 128), 128, 0, s>>>(v, g->words, h, (uint32_t)g->nwords);
+    g->ctx->launches += 2;
+    VXL_TRY_CUDA(cudaGetLastError());
+    return launch_build_tile_mask(g, s);
 }
 
 vxl_status launch_scene_boxes(vxl_grid* g, uint32_t seed, int nboxes, int smin, int smax, cudaStream_t s) {

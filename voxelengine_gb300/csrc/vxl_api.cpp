@@ -758,6 +758,15 @@ vxl_status vxl_scene_soft(vxl_ctx* ctx, float* d_soft, int nx, int ny, int nz, u
                              (cudaStream_t)stream);
 }
 
+vxl_status vxl_scene_terrain(vxl_ctx* ctx, vxl_grid* g, uint32_t seed, float base, float amplitude, float freq,
+                             int octaves, float* d_height, void* stream) {
+    if (!ctx || !grid_ok(g) || octaves < 1 || octaves > 16 || !std::isfinite(base) || !std::isfinite(amplitude) ||
+        !std::isfinite(freq))
+        return fail(VXL_ERR_INVALID_ARG, "scene_terrain: bad argument");
+    VXL_TRY(set_device(ctx));
+    return launch_scene_terrain(g, seed, base, amplitude, freq, octaves, d_height, (cudaStream_t)stream);
+}
+
 vxl_status vxl_scene_boxes(vxl_ctx* ctx, vxl_grid* g, uint32_t seed, int nboxes, int smin, int smax, void* stream) {
     if (!ctx || !grid_ok(g) || nboxes < 0 || smin < 1 || smax < smin)
         return fail(VXL_ERR_INVALID_ARG, "scene_boxes: bad argument");

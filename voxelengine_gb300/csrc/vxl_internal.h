@@ -77,6 +77,8 @@ vxl_status launch_build_tile_mask(vxl_grid* g, cudaStream_t s);
 vxl_status launch_grid_count(const vxl_grid* g, unsigned long long* d_out, cudaStream_t s);
 vxl_status launch_scene_noise(vxl_grid* g, uint32_t seed, float thresh, float freq, int ground_y, cudaStream_t s);
 vxl_status launch_scene_boxes(vxl_grid* g, uint32_t seed, int nboxes, int smin, int smax, cudaStream_t s);
+vxl_status launch_scene_terrain(vxl_grid* g, uint32_t seed, float base, float amp, float freq, int octaves,
+                                float* d_height, cudaStream_t s);
 vxl_status launch_scene_soft(vxl_ctx* ctx, float* soft, int nx, int ny, int nz, uint32_t seed, float thresh,
                              float sharpness, float freq, int ground_y, uint32_t albedo_seed, cudaStream_t s);
 vxl_status launch_soft_fwd(vxl_ctx* ctx, const float* soft, int nx, int ny, int nz, const vxl_gbuffer* gb,

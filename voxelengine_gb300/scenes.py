@@ -142,3 +142,62 @@ def instance_set(scenes, n_instances, models, seed):
         mi = int(rng.integers(0, len(models)))
         per[s].append((instance_matrix(rng, scenes[s]["n"], models[mi].shape), mi, V.OP_SET))
     return per
+
+
+def terrain_camera(n, top):
+    """Above the terrain's near edge, looking down across it."""
+    cam = np.array([0.5 * n, top + 0.35 * n, -0.15 * n], np.float32)
+    tgt = np.array([0.5 * n, 0.5 * top, 0.55 * n], np.float32)
+    return cam, tgt
+
+
+def make_terrain_scene(ctx, n=2048, W=3840, H=2160, seed=5, n_instances=50000, n_models=48, edge=(16, 128),
+                       base=None, amplitude=512.0, freq=None, octaves=6, params=None):
+    """Stress scene: n^3 grid with a heightfield terrain (base + amplitude * fbm,
+    `octaves` octaves) and n_instances Vox-model instances (edges in `edge`,
+    uniform rotations) standing on the terrain, voxelized on the device;
+    W x H G-buffer; 1 shadow ray, 16 AO rays of length 64 and 1 specular ray."""
+    import torch
+
+    base = n / 16.0 if base is None else base
+    freq = 1.0 / (n / 4.0) if freq is None else freq
+    G = V.Grid(ctx, n, n, n)
+    d_h = torch.empty((n, n), dtype=torch.float32, device="cuda")
+    G.scene_terrain(seed, base, amplitude, freq, octaves, d_height=d_h)
+    h = d_h.cpu().numpy()
+    models = vox_models(seed + 1, n_models, edge[0], edge[1], fill=0.4)
+    d_models = [torch.from_numpy(m).cuda() for m in models]
+    mdesc = [(d.data_ptr(),) + m.shape[::-1] for m, d in zip(models, d_models)]
+    rng = np.random.default_rng(seed + 2)
+    insts = []
+    for _ in range(n_instances):
+        mi = int(rng.integers(0, n_models))
+        sz, sy, sx = models[mi].shape
+        x, z = rng.uniform(0, n - 1, 2)
+        y = float(h[int(z), int(x)]) - 0.25 * sy  # a quarter sunk into the ground
+        m = np.eye(4)
+        R = rotation_matrix(rng)
+        m[:3, :3] = R
+        half = 0.05 * np.array([sx, sy, sz])
+        m[:3, 3] = np.array([x, y, z]) / 10.0 - R @ half
+        insts.append((np.ascontiguousarray(m.T.astype(np.float32)).reshape(16), mi, V.OP_SET))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    V.voxelize(ctx, G, mdesc, insts)
+    e1.record()
+    torch.cuda.synchronize()
+    vox_s = e0.elapsed_time(e1) / 1e3
+    top = float(h.max()) + amplitude * 0.1
+    cam, tgt = terrain_camera(n, top)
+    npix = W * H
+    pos = torch.empty(npix * 3, dtype=torch.float32, device="cuda")
+    nrm = torch.empty_like(pos)
+    rough = torch.empty(npix, dtype=torch.float32, device="cuda")
+    V.scene_gbuffer(ctx, G, cam, tgt, W, H, seed, pos, nrm, rough)
+    P = params or V.make_params(light_dir=light_dir(seed), cam_pos=cam, bias=0.5, shadow_len=256.0, ao_len=64.0,
+                                spec_len=256.0, n_shadow=1, n_ao=16, n_spec=1, seed=seed)
+    src_voxels = sum(int(models[mi].size) for _, mi, _ in insts)
+    return dict(grid=G, n=n, W=W, H=H, width=W, height=H, npix=npix, pos=pos, nrm=nrm, rough=rough, params=P,
+                cam=cam, seed=seed, heights=d_h, models=models, d_models=d_models, mdesc=mdesc, instances=insts,
+                voxelize_seconds=vox_s, source_voxels=src_voxels)
