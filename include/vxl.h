@@ -358,6 +358,63 @@ vxl_status vxl_trace_soft_bwd(vxl_ctx* ctx, const float* d_soft, int nx, int ny,
                               const vxl_soft_params* p, const float* d_grad_image, const float* d_light,
                               float* d_grad_soft, void* stream);
 
+/* ------------------------------------------------- primary visibility
+ * Replaces GeometryVoxelPipeline::Use (GeometryVoxelPipeline.h:50-70) with
+ * GeometryVoxel.{vert,frag}: per pixel, the nearest voxel hit over all
+ * instances, as a G-buffer for vxl_trace_occlusion. */
+/* A VoxAsset image with its mips (VoxAsset.h:26-31, VoxAsset.cpp:3-63):
+ * device R8 palette indices, mip m of size max(1, s >> m) per axis
+ * (p > 1 ? p / 2 : 1), x fastest. VoxAsset rounds sizes up to multiples of 4;
+ * here each size must be >= 4. */
+typedef struct vxl_volume {
+    const uint8_t* mip[3];
+    int32_t sx, sy, sz;
+    int32_t pad;
+} vxl_volume;
+/* Build mips 1 and 2 from mip 0 (VoxAsset::Upload's first-non-zero-child rule). */
+vxl_status vxl_volume_build_mips(vxl_ctx* ctx, const uint8_t* d_mip0, int sx, int sy, int sz, uint8_t* d_mip1,
+                                 uint8_t* d_mip2, void* stream);
+/* GeometryVoxelPipeline::Cmd (GeometryVoxelPipeline.h:30-36): world matrix
+ * (column-major; WorldMatrix * translate(-Pivot), WorldRenderer.cpp:213-218)
+ * mapping volume voxel v to world units as world = R (v * 0.1) + t (its
+ * projective row is ignored), the volume (index into the volume table) and
+ * the palette index (passed through, not used here). */
+typedef struct vxl_voxcmd {
+    float world[16];
+    int32_t volume;
+    int32_t palette;
+} vxl_voxcmd;
+/* Pinhole camera in world units: pixel (px, py) looks along
+ * normalize(fwd + right * u + up * v), u = ((px + .5) * 2 / W - 1) * tan_half_fov * W / H,
+ * v = (1 - (py + .5) * 2 / H) * tan_half_fov, fwd = normalize(target - pos),
+ * right = normalize(cross(fwd, (0,1,0))), up = cross(right, fwd) (as
+ * vxl_scene_gbuffer). frame = GetFrame() (dithers glass voxels, palette < 16). */
+typedef struct vxl_camera {
+    float pos[3];
+    float target[3];
+    float tan_half_fov;
+    int32_t width, height;
+    int32_t frame;
+} vxl_camera;
+/* Outputs, device, [W*H] row-major; NULL to skip (pos and nrm are required).
+ * Sky pixels: pos = nrm = 0, depth = 0, material = 0, instance = -1. */
+typedef struct vxl_primary_out {
+    float* pos;          /* [npix][3] hit position in fine-voxel units (world * 10) */
+    float* nrm;          /* [npix][3] world normal */
+    float* depth;        /* [npix] view depth along fwd, world units */
+    int32_t* material;   /* [npix] palette index of the hit voxel */
+    int32_t* instance;   /* [npix] index of the hit command */
+} vxl_primary_out;
+/* Per pixel: for every command whose volume box [0, dims] the pixel ray
+ * (moved into the volume's space: local = R^-1 (p - t) * 10) enters,
+ * clipToAABB + intersectVolume (GeometryVoxel.frag:50-125, LOD and
+ * transparency on, UV = ((px + .5) * 2 / W - 1, (py + .5) * 2 / H - 1)); the
+ * nearest hit by view depth wins, ties to the lower command index. Host
+ * arrays; returns after one read-back (the screen-bin size) with the frame
+ * queued on `stream`. */
+vxl_status vxl_trace_primary(vxl_ctx* ctx, const vxl_volume* volumes, int nvolumes, const vxl_voxcmd* cmds, int ncmds,
+                             const vxl_camera* camera, const vxl_primary_out* out, void* stream);
+
 /* .v asset reader (VoxAsset::Serialize, VoxAsset.h:42-50): u32 sx,sy,sz then
  * sx*sy*sz bytes. Query with data == NULL to get the sizes, then read into a
  * host buffer of sx*sy*sz bytes. */

@@ -139,6 +139,13 @@ def lib():
                                            ip]
             L.vo_fnv1a64.restype = C.c_uint64
             L.vo_fnv1a64.argtypes = [C.c_char_p]
+            L.vo_volume_mips.argtypes = [u8p, C.c_int, C.c_int, C.c_int, u8p, u8p]
+            L.vo_clip_intersect.argtypes = [u8p, u8p, u8p, C.c_int, C.c_int, C.c_int, fp, fp, fp, C.c_float,
+                                            C.c_float, C.c_float, C.c_float, C.c_int, C.c_int, fp, fp,
+                                            C.POINTER(C.c_uint32), ip]
+            L.vo_affine_inverse.argtypes = [fp, fp, fp]
+            L.vo_primary.argtypes = [vp, vp, vp, ip, fp, ip, C.c_int, fp, fp, C.c_float, C.c_int, C.c_int, C.c_int,
+                                     fp, fp, fp, ip, ip, C.c_int]
             L.vo_soft_render.argtypes = [fp, C.c_int, C.c_int, C.c_int, fp, fp, C.c_int, C.POINTER(SoftParams),
                                          vp, C.c_int64, C.c_double, vp, vp, C.c_int]
             _lib = L
@@ -421,6 +428,77 @@ def vox_destroyed(g, model, world):
 
 def fnv1a64(s: str) -> int:
     return lib().vo_fnv1a64(s.encode())
+
+
+# ------------------------------------------------------ primary visibility
+def mip_dims(s):
+    """mip sizes of VoxAsset::Upload: p > 1 ? p / 2 : 1, per axis; s = (sx, sy, sz)"""
+    d = [tuple(s)]
+    for _ in range(2):
+        d.append(tuple(v // 2 if v > 1 else 1 for v in d[-1]))
+    return d
+
+
+def volume_mips(vol):
+    """vol uint8[sz, sy, sx] -> (mip1, mip2) as arrays [z, y, x] (VoxAsset::Upload)."""
+    vol = np.ascontiguousarray(vol, np.uint8)
+    sz, sy, sx = vol.shape
+    d = mip_dims((sx, sy, sz))
+    m1 = np.zeros(d[1][::-1], np.uint8)
+    m2 = np.zeros(d[2][::-1], np.uint8)
+    lib().vo_volume_mips(_u8(vol), sx, sy, sz, _u8(m1), _u8(m2))
+    return m1, m2
+
+
+def clip_intersect(mips, origin, direction, lcam, uv=(0.0, 0.0), res=(1.0, 1.0), frame=0, clip=True):
+    """intersectVolume (after clipToAABB when clip) on a volume given as its 3 mips [z, y, x];
+    returns (hit, hitpos[3], normal[3], material, fetches)."""
+    m0, m1, m2 = (np.ascontiguousarray(m, np.uint8) for m in mips)
+    sz, sy, sx = m0.shape
+    h = np.zeros(3, np.float32)
+    nrm = np.zeros(3, np.float32)
+    mat = C.c_uint32()
+    fe = C.c_int()
+    o = np.asarray(origin, np.float32)
+    d = np.asarray(direction, np.float32)
+    lc = np.asarray(lcam, np.float32)
+    r = lib().vo_clip_intersect(_u8(m0), _u8(m1), _u8(m2), sx, sy, sz, _f(o), _f(d), _f(lc), uv[0], uv[1], res[0],
+                                res[1], frame, 1 if clip else 0, _f(h), _f(nrm), C.byref(mat), C.byref(fe))
+    return r, h, nrm, mat.value, fe.value
+
+
+def affine_inverse(m16):
+    m = np.ascontiguousarray(m16, np.float32).reshape(16)
+    ri = np.zeros(9, np.float32)
+    ti = np.zeros(3, np.float32)
+    lib().vo_affine_inverse(_f(m), _f(ri), _f(ti))
+    return ri, ti
+
+
+def primary(volumes, worlds, vol_of, cam, target, W, H, frame=0, tan_half_fov=0.57735026, threads=None):
+    """Per-pixel primary visibility. volumes: list of uint8[sz, sy, sx] (mip 0);
+    worlds: float32[n, 16] column-major; vol_of: int[n]. Camera in world units.
+    Returns dict pos[npix,3] (fine units), nrm, depth, material, instance."""
+    vols = [np.ascontiguousarray(v, np.uint8) for v in volumes]
+    mips = [volume_mips(v) for v in vols]
+    keep = vols + [m for mm in mips for m in mm]
+    p0 = (C.c_void_p * len(vols))(*[v.ctypes.data for v in vols])
+    p1 = (C.c_void_p * len(vols))(*[m[0].ctypes.data for m in mips])
+    p2 = (C.c_void_p * len(vols))(*[m[1].ctypes.data for m in mips])
+    dims = np.array([v.shape[::-1] for v in vols], np.int32).reshape(-1)
+    worlds = np.ascontiguousarray(worlds, np.float32).reshape(-1, 16)
+    vol_of = np.ascontiguousarray(vol_of, np.int32)
+    n = W * H
+    out = dict(pos=np.zeros((n, 3), np.float32), nrm=np.zeros((n, 3), np.float32), depth=np.zeros(n, np.float32),
+               material=np.zeros(n, np.int32), instance=np.zeros(n, np.int32))
+    c = np.asarray(cam, np.float32)
+    t = np.asarray(target, np.float32)
+    lib().vo_primary(C.cast(p0, C.c_void_p), C.cast(p1, C.c_void_p), C.cast(p2, C.c_void_p), _i(dims), _f(worlds),
+                     _i(vol_of), worlds.shape[0], _f(c), _f(t), C.c_float(tan_half_fov), W, H, frame,
+                     _f(out["pos"]), _f(out["nrm"]), _f(out["depth"]), _i(out["material"]), _i(out["instance"]),
+                     threads or threads_default())
+    del keep
+    return out
 
 
 def make_soft_params(light_dir=(0.3, 0.8, 0.5), bias=0.5, length=24.0, k_sun=0.7, k_amb=0.5, n_shadow=1,

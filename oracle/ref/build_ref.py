@@ -17,6 +17,10 @@ output into oracle/_ref/ (git-ignored):
   compiled inside wrapper functions of the harness.
 * Sources/World/Systems/ShadowVoxSystem.cpp is compiled unmodified against the
   stand-in headers in oracle/ref/shim/ (engine, Vulkan and entt types).
+* clipToAABB and intersectVolume are cut out of Sources/Shaders/GeometryVoxel.frag
+  (same two edits, plus `out uint` -> `uint&`) and compiled inside
+  ref_geometry_harness.cpp with a three-mip R8 volume; the mip loop of
+  VoxAsset::Upload (Sources/Asset/VoxAsset.cpp) is cut out and compiled there too.
 
 Compiler flags: -O2 -ffp-contract=off -fsingle-precision-constant (GLSL float
 literals are single precision). Output: oracle/_ref/libvxl_ref.so.
@@ -47,6 +51,7 @@ def available() -> bool:
 
 def _glslpp(text: str) -> str:
     text = re.sub(r"\bout\s+vec3\s+", "vec3& ", text)
+    text = re.sub(r"\bout\s+uint\s+", "uint& ", text)
     text = re.sub(r"\.([xyzw]{2,4})\b(?!\s*\()", r".\1()", text)
     return text
 
@@ -72,6 +77,22 @@ def _block(src: str, start: str, end: str) -> str:
     return "\n".join(lines[s : e + 1])
 
 
+def _braced_from(src: str, start: str) -> str:
+    """From the line holding `start` to the brace that closes the block it opens."""
+    i = src.index(start)
+    i = src.rindex("\n", 0, i) + 1
+    j = src.index("{", i)
+    depth = 0
+    for k in range(j, len(src)):
+        if src[k] == "{":
+            depth += 1
+        elif src[k] == "}":
+            depth -= 1
+            if depth == 0:
+                return src[i : k + 1]
+    raise ValueError("unbalanced braces after " + start)
+
+
 def generate() -> None:
     r = reference_dir()
     sh = os.path.join(r, "Sources", "Shaders")
@@ -81,7 +102,12 @@ def generate() -> None:
     refl = open(os.path.join(sh, "LightReflection.frag")).read()
     point = open(os.path.join(sh, "LightPoint.frag")).read()
     spot = open(os.path.join(sh, "LightSpot.frag")).read()
+    geo = open(os.path.join(sh, "GeometryVoxel.frag")).read()
+    voxasset = open(os.path.join(r, "Sources", "Asset", "VoxAsset.cpp")).read()
     parts = {
+        "geometry_clip.inc": _glslpp(_function(geo, "vec3 clipToAABB(")),
+        "geometry_intersect.inc": _glslpp(_function(geo, "bool intersectVolume(")),
+        "voxasset_mip.inc": _braced_from(voxasset, "for (int x = 0; x < mipSizeX; x++)"),
         "Light_frag.inc": _glslpp(light),
         "ambient_cosine.inc": _glslpp(_function(amb, "vec3 cosineSampleHemisphere(")),
         "ambient_irradiance.inc": _glslpp(_function(amb, "vec3 calculateAmbientIrradiance(")),
@@ -107,7 +133,8 @@ def build(force: bool = False, verbose: bool = False) -> str | None:
     """Build oracle/_ref/libvxl_ref.so; returns its path, or None if the reference is absent."""
     if not available():
         return None
-    srcs = [os.path.join(HERE, "ref_light_harness.cpp"), os.path.join(HERE, "ref_voxelizer_harness.cpp")]
+    srcs = [os.path.join(HERE, "ref_light_harness.cpp"), os.path.join(HERE, "ref_voxelizer_harness.cpp"),
+            os.path.join(HERE, "ref_geometry_harness.cpp")]
     if not force and os.path.exists(SO) and os.path.getmtime(SO) >= max(os.path.getmtime(s) for s in srcs + [__file__]):
         return SO
     generate()
@@ -130,6 +157,10 @@ def build(force: bool = False, verbose: bool = False) -> str | None:
     subprocess.run(common + ["-c", "-I", os.path.join(HERE, "shim"), "-I", os.path.join(r, "Vendor"),
                              "-I", os.path.join(r, "Sources", "World", "Systems"), srcs[1], "-o", o3], check=True)
     objs.append(o3)
+    # GeometryVoxel.frag's clipToAABB / intersectVolume and VoxAsset::Upload's mip loop
+    o4 = os.path.join(OUT, "ref_geometry.o")
+    subprocess.run(common + ["-c", "-I", OUT, "-I", os.path.join(r, "Vendor"), srcs[2], "-o", o4], check=True)
+    objs.append(o4)
     tmp = SO + ".tmp%d" % os.getpid()
     subprocess.run(["g++", "-shared", "-o", tmp] + objs, check=True)
     os.replace(tmp, SO)

@@ -1086,3 +1086,290 @@ extern "C" void vo_soft_render(const float* vox, int nx, int ny, int nz, const f
         grad_vox[k] = s;
     }
 }
+
+// ===========================================================================
+// Primary visibility: the G-buffer producer of GeometryVoxel.{vert,frag}.
+namespace {
+
+// VoxAsset::Upload, Sources/Asset/VoxAsset.cpp:3-63: a voxel of mip m+1 is the
+// first non-zero of its children at mip m, probed in the order vi = 0..8
+// (child (2x + (vi&1), 2y + (vi>>1&1), 2z + (vi>>2&1)); vi = 8 repeats vi = 0).
+void mip_down(const uint8_t* parent, int psx, int psy, uint8_t* child, int csx, int csy, int csz) {
+    for (int x = 0; x < csx; x++)
+        for (int y = 0; y < csy; y++)
+            for (int z = 0; z < csz; z++) {
+                uint8_t vox = 0;
+                for (int vi = 0; vi < 9; vi++) {
+                    const uint8_t up = parent[(size_t)(2 * x + ((vi >> 0) & 1)) +
+                                              (size_t)(2 * y + ((vi >> 1) & 1)) * psx +
+                                              (size_t)(2 * z + ((vi >> 2) & 1)) * psx * psy];
+                    if (up) {
+                        vox = up;
+                        break;
+                    }
+                }
+                child[(size_t)x + (size_t)y * csx + (size_t)z * csx * csy] = vox;
+            }
+}
+inline int mip_dim(int d) { return d > 1 ? d / 2 : 1; }
+
+struct Volume {
+    const uint8_t* m[3];
+    int sx[3], sy[3], sz[3];
+    // texelFetch(VOLUME_TEXTURE, p, mip).r with robust out-of-range = 0
+    inline uint32_t texel(int mip, int x, int y, int z) const {
+        if (x < 0 || y < 0 || z < 0 || x >= sx[mip] || y >= sy[mip] || z >= sz[mip]) return 0u;
+        return m[mip][(size_t)x + (size_t)y * sx[mip] + (size_t)z * sx[mip] * sy[mip]];
+    }
+};
+
+// glm's scalar max / min: (x < y) ? y : x and (y < x) ? y : x
+inline float gmax(float x, float y) { return (x < y) ? y : x; }
+inline float gmin(float x, float y) { return (y < x) ? y : x; }
+
+// clipToAABB, Sources/Shaders/GeometryVoxel.frag:50-61
+V3 clip_to_aabb(V3 o, V3 d, V3 size) {
+    const V3 c = v3(gmin(gmax(o.x, 0.0f), size.x), gmin(gmax(o.y, 0.0f), size.y), gmin(gmax(o.z, 0.0f), size.z));
+    if (c.x == o.x && c.y == o.y && c.z == o.z) return o;
+    const V3 inv = v3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    const V3 sgn = v3(glsl_step(d.x, 0.0f), glsl_step(d.y, 0.0f), glsl_step(d.z, 0.0f));
+    const V3 t = mulv(sub(mulv(sgn, size), o), inv);
+    const float tmin = gmax(gmax(t.x, t.y), t.z);
+    return add(o, mul(d, tmin - 0.001f));
+}
+
+// intersectVolume, Sources/Shaders/GeometryVoxel.frag:63-125, with LOD 1,
+// MIP_COUNT 2 and TRANSPARENCY 1. lcam = In.localCameraPos; (uvx, uvy) the
+// fragment's UV, res = GetRes(), frame = GetFrame().
+int intersect_volume(const Volume& V, V3 origin, V3 direction, V3 lcam, float uvx, float uvy, float resx, float resy,
+                     int frame, V3* hit, V3* normal, uint32_t* material, int* fetches) {
+    const V3 ss = v3(glsl_sign(direction.x), glsl_sign(direction.y), glsl_sign(direction.z));
+    const V3 td = v3(1.0f / (direction.x * ss.x), 1.0f / (direction.y * ss.y), 1.0f / (direction.z * ss.z));
+    int mip = 2;
+    int i = 0;
+    int nf = 0;
+    do {
+        const float mipSize = (float)(1 << mip);
+        origin = v3(origin.x / mipSize, origin.y / mipSize, origin.z / mipSize);
+        int cx = (int)std::floor(origin.x), cy = (int)std::floor(origin.y), cz = (int)std::floor(origin.z);
+        const V3 nb = v3((float)cx + (ss.x * 0.5f + 0.5f), (float)cy + (ss.y * 0.5f + 0.5f),
+                         (float)cz + (ss.z * 0.5f + 0.5f));
+        V3 tm = v3((nb.x - origin.x) / direction.x, (nb.y - origin.y) / direction.y, (nb.z - origin.z) / direction.z);
+        // clamp(current_voxel, ivec3(-1), ivec3(volumeDimension/mipSize)+1)
+        const int ux = (int)((float)V.sx[0] / mipSize) + 1, uy = (int)((float)V.sy[0] / mipSize) + 1,
+                  uz = (int)((float)V.sz[0] / mipSize) + 1;
+        int n = 0;
+        bool descended = false;
+        do {
+            const float selx = glsl_step(tm.x, tm.z) * glsl_step(tm.x, tm.y);
+            const float sely = glsl_step(tm.y, tm.x) * glsl_step(tm.y, tm.z);
+            const float selz = glsl_step(tm.z, tm.y) * glsl_step(tm.z, tm.x);
+            cx += (int)(selx * ss.x);
+            cy += (int)(sely * ss.y);
+            cz += (int)(selz * ss.z);
+            if (cx < -1 || cy < -1 || cz < -1 || cx > ux || cy > uy || cz > uz) {
+                if (fetches) *fetches = nf;
+                return 0;
+            }
+            const uint32_t voxel = V.texel(mip, cx, cy, cz);
+            nf++;
+            if (voxel != 0u) {
+                float best_t = tm.x * selx + tm.y * sely;
+                best_t = best_t + tm.z * selz;
+                bool accept = mip == 0;
+                if (!accept) {
+                    const V3 p = mul(add(origin, mul(direction, best_t)), mipSize);
+                    const V3 dd = sub(p, lcam);
+                    accept = (float)mip < 0.001f * std::sqrt(dot(dd, dd));
+                }
+                if (accept) {
+                    const float kx = std::round(uvx * resx * 0.5f), ky = std::round(uvy * resy * 0.5f);
+                    const bool glass = voxel < 16u && glsl_mod(ky + kx, 2.0f) == (float)(frame % 2);
+                    if (!glass) {
+                        *normal = v3(-ss.x * selx, -ss.y * sely, -ss.z * selz);
+                        *hit = mul(add(origin, mul(direction, best_t)), mipSize);
+                        *material = voxel;
+                        if (fetches) *fetches = nf;
+                        return 1;
+                    }
+                } else {
+                    mip--;
+                    const V3 step = mul(direction, best_t);
+                    origin = add(origin, v3(step.x / mipSize, step.y / mipSize, step.z / mipSize));
+                    descended = true;
+                    break;
+                }
+            }
+            tm = v3(tm.x + td.x * selx, tm.y + td.y * sely, tm.z + td.z * selz);
+        } while (++n < 512);
+        (void)descended;
+        origin = mul(origin, mipSize);
+    } while (++i < 4);
+    if (fetches) *fetches = nf;
+    return 0;
+}
+
+// Inverse of the affine part of a column-major 4x4 (rows 0-2): R^-1 by the
+// adjugate over the determinant, t' = -R^-1 t; fixed operation order (the
+// CUDA path does the same operations).
+void affine_inverse(const float* m, float* ri, float* ti) {
+    const float a00 = m[0], a10 = m[1], a20 = m[2];
+    const float a01 = m[4], a11 = m[5], a21 = m[6];
+    const float a02 = m[8], a12 = m[9], a22 = m[10];
+    const float c00 = a11 * a22 - a12 * a21, c01 = a12 * a20 - a10 * a22, c02 = a10 * a21 - a11 * a20;
+    const float c10 = a02 * a21 - a01 * a22, c11 = a00 * a22 - a02 * a20, c12 = a01 * a20 - a00 * a21;
+    const float c20 = a01 * a12 - a02 * a11, c21 = a02 * a10 - a00 * a12, c22 = a00 * a11 - a01 * a10;
+    float det = a00 * c00 + a01 * c01;
+    det = det + a02 * c02;
+    const float id = 1.0f / det;
+    // ri row-major: ri[r*3 + c] = cofactor(c, r) / det
+    ri[0] = c00 * id; ri[1] = c10 * id; ri[2] = c20 * id;
+    ri[3] = c01 * id; ri[4] = c11 * id; ri[5] = c21 * id;
+    ri[6] = c02 * id; ri[7] = c12 * id; ri[8] = c22 * id;
+    for (int r = 0; r < 3; r++) {
+        float v = ri[r * 3 + 0] * m[12] + ri[r * 3 + 1] * m[13];
+        v = v + ri[r * 3 + 2] * m[14];
+        ti[r] = -v;
+    }
+}
+inline V3 rmul3(const float* r, V3 v) {  // row-major 3x3 times vector
+    float x = r[0] * v.x + r[1] * v.y;
+    float y = r[3] * v.x + r[4] * v.y;
+    float z = r[6] * v.x + r[7] * v.y;
+    return v3(x + r[2] * v.z, y + r[5] * v.z, z + r[8] * v.z);
+}
+inline V3 cmul3(const float* m, V3 v) {  // linear part of a column-major 4x4 times vector
+    float x = m[0] * v.x + m[4] * v.y;
+    float y = m[1] * v.x + m[5] * v.y;
+    float z = m[2] * v.x + m[6] * v.y;
+    return v3(x + m[8] * v.z, y + m[9] * v.z, z + m[10] * v.z);
+}
+
+}  // namespace
+
+extern "C" {
+
+void vo_volume_mips(const uint8_t* mip0, int sx, int sy, int sz, uint8_t* mip1, uint8_t* mip2) {
+    const int x1 = mip_dim(sx), y1 = mip_dim(sy), z1 = mip_dim(sz);
+    mip_down(mip0, sx, sy, mip1, x1, y1, z1);
+    mip_down(mip1, x1, y1, mip2, mip_dim(x1), mip_dim(y1), mip_dim(z1));
+}
+
+int vo_clip_intersect(const uint8_t* mip0, const uint8_t* mip1, const uint8_t* mip2, int sx, int sy, int sz,
+                      const float* origin, const float* dir, const float* lcam, float uvx, float uvy, float resx,
+                      float resy, int frame, int clip, float* hit, float* normal, uint32_t* material, int* fetches) {
+    Volume V;
+    V.m[0] = mip0;
+    V.m[1] = mip1;
+    V.m[2] = mip2;
+    V.sx[0] = sx; V.sy[0] = sy; V.sz[0] = sz;
+    for (int k = 1; k < 3; k++) {
+        V.sx[k] = mip_dim(V.sx[k - 1]);
+        V.sy[k] = mip_dim(V.sy[k - 1]);
+        V.sz[k] = mip_dim(V.sz[k - 1]);
+    }
+    V3 o = load3(origin), d = load3(dir);
+    if (clip) o = clip_to_aabb(o, d, v3((float)sx, (float)sy, (float)sz));
+    V3 h = v3(0, 0, 0), nrm = v3(0, 0, 0);
+    uint32_t mat = 0;
+    const int r = intersect_volume(V, o, d, load3(lcam), uvx, uvy, resx, resy, frame, &h, &nrm, &mat, fetches);
+    hit[0] = h.x; hit[1] = h.y; hit[2] = h.z;
+    normal[0] = nrm.x; normal[1] = nrm.y; normal[2] = nrm.z;
+    *material = mat;
+    return r;
+}
+
+void vo_affine_inverse(const float* m, float* ri, float* ti) { affine_inverse(m, ri, ti); }
+
+// Per-pixel primary visibility over instances (GeometryVoxelPipeline::Use,
+// GeometryVoxelPipeline.h:50-70, resolved by depth): the pixel ray of the
+// vxl_scene_gbuffer camera, in world units, is moved into each instance's
+// volume space (local = R^-1 (p - t) * 10, direction R^-1 d normalized),
+// tested against the volume box [0, dims] and, where it enters, clipped
+// (clipToAABB) and traced (intersectVolume); the nearest hit by view depth
+// wins, ties to the lower instance index.
+void vo_primary(const uint8_t* const* mip0s, const uint8_t* const* mip1s, const uint8_t* const* mip2s,
+                const int* vdims, const float* worlds, const int* vol_of, int ninst, const float* cam_in,
+                const float* target, float tan_half_fov, int W, int H, int frame, float* pos, float* nrm,
+                float* depth, int32_t* material, int32_t* instance, int threads) {
+    const V3 cam = load3(cam_in);
+    const V3 fwd = normalize(sub(load3(target), cam));
+    const V3 right = normalize(cross(fwd, v3(0.0f, 1.0f, 0.0f)));
+    const V3 upv = cross(right, fwd);
+    const float aspect = (float)W / (float)H;
+    std::vector<float> rinv((size_t)ninst * 9), tinv((size_t)ninst * 3);
+    for (int k = 0; k < ninst; k++) affine_inverse(worlds + 16 * (size_t)k, &rinv[9 * (size_t)k], &tinv[3 * (size_t)k]);
+    parallel_for(W * H, threads, [&](int i) {
+        const int px = i % W, py = i / W;
+        const float uvx = ((float)px + 0.5f) * 2.0f / (float)W - 1.0f;
+        const float uvy = ((float)py + 0.5f) * 2.0f / (float)H - 1.0f;
+        const float u = uvx * tan_half_fov * aspect;
+        const float v = (1.0f - ((float)py + 0.5f) * 2.0f / (float)H) * tan_half_fov;
+        const V3 d = normalize(add(add(fwd, mul(right, u)), mul(upv, v)));
+        float best = 0.0f;
+        int bi = -1;
+        V3 bp = v3(0, 0, 0), bn = v3(0, 0, 0);
+        uint32_t bm = 0;
+        for (int k = 0; k < ninst; k++) {
+            const float* M = worlds + 16 * (size_t)k;
+            const float* ri = &rinv[9 * (size_t)k];
+            const float* ti = &tinv[3 * (size_t)k];
+            const int vi = vol_of[k];
+            const int sx = vdims[3 * vi], sy = vdims[3 * vi + 1], sz = vdims[3 * vi + 2];
+            V3 lc = rmul3(ri, cam);
+            lc = mul(add(lc, v3(ti[0], ti[1], ti[2])), 10.0f);
+            const V3 ld = normalize(rmul3(ri, d));
+            // the pixel's ray enters the volume box (what rasterizing its cube covers)
+            const float dims[3] = {(float)sx, (float)sy, (float)sz};
+            const float lo[3] = {lc.x, lc.y, lc.z}, dl[3] = {ld.x, ld.y, ld.z};
+            float t0 = -INFINITY, t1 = INFINITY;
+            for (int a = 0; a < 3; a++) {
+                const float inv = 1.0f / dl[a];
+                const float ta = (0.0f - lo[a]) * inv, tb = (dims[a] - lo[a]) * inv;
+                t0 = std::fmax(t0, std::fmin(ta, tb));
+                t1 = std::fmin(t1, std::fmax(ta, tb));
+            }
+            if (!(t0 <= t1 && t1 >= 0.0f)) continue;
+            Volume V;
+            V.m[0] = mip0s[vi];
+            V.m[1] = mip1s[vi];
+            V.m[2] = mip2s[vi];
+            V.sx[0] = sx; V.sy[0] = sy; V.sz[0] = sz;
+            for (int q = 1; q < 3; q++) {
+                V.sx[q] = mip_dim(V.sx[q - 1]);
+                V.sy[q] = mip_dim(V.sy[q - 1]);
+                V.sz[q] = mip_dim(V.sz[q - 1]);
+            }
+            const V3 o = clip_to_aabb(lc, ld, v3(dims[0], dims[1], dims[2]));
+            V3 h, nn;
+            uint32_t mat;
+            if (!intersect_volume(V, o, ld, lc, uvx, uvy, (float)W, (float)H, frame, &h, &nn, &mat, nullptr)) continue;
+            // world position (world units) of the hit, its view depth
+            const V3 wl = cmul3(M, mul(h, 0.1f));
+            const V3 wp = v3(wl.x + M[12], wl.y + M[13], wl.z + M[14]);
+            const float dep = dot(sub(wp, cam), fwd);
+            if (bi < 0 || dep < best) {
+                best = dep;
+                bi = k;
+                bp = wp;
+                bn = normalize(cmul3(M, nn));
+                bm = mat;
+            }
+        }
+        float* po = pos + 3 * (size_t)i;
+        float* no = nrm + 3 * (size_t)i;
+        if (bi >= 0) {
+            po[0] = bp.x * 10.0f; po[1] = bp.y * 10.0f; po[2] = bp.z * 10.0f;
+            no[0] = bn.x; no[1] = bn.y; no[2] = bn.z;
+            depth[i] = best;
+        } else {
+            po[0] = po[1] = po[2] = 0.0f;
+            no[0] = no[1] = no[2] = 0.0f;
+            depth[i] = 0.0f;
+        }
+        material[i] = (int32_t)bm;
+        instance[i] = bi;
+    });
+}
+
+}  // extern "C"

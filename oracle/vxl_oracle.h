@@ -148,6 +148,20 @@ void vo_soft_render(const float* vox, int nx, int ny, int nz, const float* pos, 
                     const vo_soft_params* p, const float* grad_image, int64_t perturb_voxel, double perturb_delta,
                     double* image, double* grad_vox, int threads);
 
+/* Primary visibility (GeometryVoxel.frag / VoxAsset.cpp) */
+/* VoxAsset::Upload mips (VoxAsset.cpp:3-63): mip1/mip2 of an R8 volume */
+void vo_volume_mips(const uint8_t* mip0, int sx, int sy, int sz, uint8_t* mip1, uint8_t* mip2);
+/* [clipToAABB then] intersectVolume (GeometryVoxel.frag:50-61, :63-125) */
+int vo_clip_intersect(const uint8_t* mip0, const uint8_t* mip1, const uint8_t* mip2, int sx, int sy, int sz,
+                      const float* origin, const float* dir, const float* lcam, float uvx, float uvy, float resx,
+                      float resy, int frame, int clip, float* hit, float* normal, uint32_t* material, int* fetches);
+void vo_affine_inverse(const float* m, float* ri, float* ti);
+/* per-pixel primary visibility over instances; camera in world units, pos out in fine units (x10) */
+void vo_primary(const uint8_t* const* mip0s, const uint8_t* const* mip1s, const uint8_t* const* mip2s,
+                const int* vdims, const float* worlds, const int* vol_of, int ninst, const float* cam,
+                const float* target, float tan_half_fov, int W, int H, int frame, float* pos, float* nrm,
+                float* depth, int32_t* material, int32_t* instance, int threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -40,7 +40,7 @@ EXPORTED = [
     "vxl_batch_run", "vxl_batch_destroy", "vxl_batch_info", "vxl_light_ambient",
     "vxl_light_reflection", "vxl_light_point", "vxl_voxelize", "vxl_voxelize_noalloc", "vxl_shadowvox_update",
     "vxl_vox_destroyed",
-    "vxl_trace_soft_fwd", "vxl_trace_soft_bwd",
+    "vxl_trace_soft_fwd", "vxl_trace_soft_bwd", "vxl_volume_build_mips", "vxl_trace_primary",
     "vxl_read_v", "vxl_scene_soft", "vxl_scene_terrain", "vxl_scene_noise", "vxl_scene_boxes", "vxl_scene_gbuffer",
 ]
 
@@ -89,6 +89,25 @@ class BatchItem(C.Structure):
 class SoftParams(C.Structure):
     _fields_ = [("light_dir", C.c_float * 3), ("bias", C.c_float), ("len", C.c_float), ("k_sun", C.c_float),
                 ("k_amb", C.c_float), ("n_shadow", C.c_int32), ("n_ao", C.c_int32), ("seed", C.c_uint32)]
+
+
+class Volume(C.Structure):
+    _fields_ = [("mip", C.c_void_p * 3), ("sx", C.c_int32), ("sy", C.c_int32), ("sz", C.c_int32),
+                ("pad", C.c_int32)]
+
+
+class VoxCmd(C.Structure):
+    _fields_ = [("world", C.c_float * 16), ("volume", C.c_int32), ("palette", C.c_int32)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("pos", C.c_float * 3), ("target", C.c_float * 3), ("tan_half_fov", C.c_float), ("width", C.c_int32),
+                ("height", C.c_int32), ("frame", C.c_int32)]
+
+
+class PrimaryOut(C.Structure):
+    _fields_ = [("pos", C.c_void_p), ("nrm", C.c_void_p), ("depth", C.c_void_p), ("material", C.c_void_p),
+                ("instance", C.c_void_p)]
 
 
 class Model(C.Structure):
@@ -159,6 +178,9 @@ def lib():
         L.vxl_vox_destroyed.argtypes = [vp, vp, C.POINTER(Model), C.POINTER(f * 16), vp, vp]
         L.vxl_read_v.argtypes = [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), vp,
                                  C.c_size_t]
+        L.vxl_volume_build_mips.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp]
+        L.vxl_trace_primary.argtypes = [vp, C.POINTER(Volume), C.c_int, C.POINTER(VoxCmd), C.c_int, C.POINTER(Camera),
+                                        C.POINTER(PrimaryOut), vp]
         L.vxl_trace_soft_fwd.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.POINTER(GBuffer), C.POINTER(SoftParams),
                                          vp, vp, vp]
         L.vxl_trace_soft_bwd.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.POINTER(GBuffer), C.POINTER(SoftParams),
@@ -436,6 +458,57 @@ def scene_soft(ctx, soft, seed, thresh=0.55, sharpness=8.0, freq=1.0 / 32.0, gro
     nx, ny, nz = _soft_dims(soft)
     check(lib().vxl_scene_soft(ctx.handle, _ptr(soft), nx, ny, nz, seed, thresh, sharpness, freq, ground_y,
                                albedo_seed, _stream(stream)))
+
+
+def volume_build_mips(ctx, d_mip0, sx, sy, sz, d_mip1, d_mip2, stream=None):
+    check(lib().vxl_volume_build_mips(ctx.handle, _ptr(d_mip0), sx, sy, sz, _ptr(d_mip1), _ptr(d_mip2),
+                                      _stream(stream)))
+
+
+class VolumeSet:
+    """Device copies of VoxAsset volumes (uint8 [sz, sy, sx] each) with their mips."""
+
+    def __init__(self, ctx, volumes):
+        import torch
+
+        self.mips = []
+        for v in volumes:
+            v = np.ascontiguousarray(v, np.uint8)
+            sz, sy, sx = v.shape
+            d0 = torch.from_numpy(v).cuda()
+            dims = [(sx, sy, sz)]
+            for _ in range(2):
+                dims.append(tuple(a // 2 if a > 1 else 1 for a in dims[-1]))
+            d1 = torch.empty(int(np.prod(dims[1])), dtype=torch.uint8, device="cuda")
+            d2 = torch.empty(int(np.prod(dims[2])), dtype=torch.uint8, device="cuda")
+            volume_build_mips(ctx, d0, sx, sy, sz, d1, d2)
+            self.mips.append((d0, d1, d2, (sx, sy, sz)))
+        self.table = (Volume * max(1, len(self.mips)))()
+        for i, (d0, d1, d2, (sx, sy, sz)) in enumerate(self.mips):
+            self.table[i].mip[:] = [d0.data_ptr(), d1.data_ptr(), d2.data_ptr()]
+            self.table[i].sx, self.table[i].sy, self.table[i].sz = sx, sy, sz
+
+    def __len__(self):
+        return len(self.mips)
+
+
+def trace_primary(ctx, volset: VolumeSet, worlds, vol_of, cam, target, W, H, pos, nrm, depth=None, material=None,
+                  instance=None, frame=0, tan_half_fov=0.57735026, stream=None):
+    """vxl_trace_primary; worlds float[n, 16] column-major, vol_of int[n]; camera in world units."""
+    worlds = np.ascontiguousarray(worlds, np.float32).reshape(-1, 16)
+    n = worlds.shape[0]
+    cmds = (VoxCmd * max(1, n))()
+    for k in range(n):
+        cmds[k].world[:] = [float(x) for x in worlds[k]]
+        cmds[k].volume = int(vol_of[k])
+        cmds[k].palette = 0
+    c = Camera()
+    c.pos[:] = [float(x) for x in cam]
+    c.target[:] = [float(x) for x in target]
+    c.tan_half_fov, c.width, c.height, c.frame = tan_half_fov, W, H, frame
+    out = PrimaryOut(_ptr(pos), _ptr(nrm), _ptr(depth), _ptr(material), _ptr(instance))
+    check(lib().vxl_trace_primary(ctx.handle, volset.table, len(volset), cmds, n, C.byref(c), C.byref(out),
+                                  _stream(stream)))
 
 
 def _models(models):

@@ -749,6 +749,36 @@ vxl_status vxl_trace_soft_bwd(vxl_ctx* ctx, const float* d_soft, int nx, int ny,
                            (cudaStream_t)stream);
 }
 
+vxl_status vxl_volume_build_mips(vxl_ctx* ctx, const uint8_t* d_mip0, int sx, int sy, int sz, uint8_t* d_mip1,
+                                 uint8_t* d_mip2, void* stream) {
+    if (!ctx || !d_mip0 || !d_mip1 || !d_mip2) return fail(VXL_ERR_INVALID_ARG, "volume_build_mips: NULL argument");
+    if (sx < 4 || sy < 4 || sz < 4 || (int64_t)sx * sy * sz > (int64_t)INT32_MAX)
+        return fail(VXL_ERR_INVALID_ARG, "volume_build_mips: sizes must be >= 4");
+    VXL_TRY(set_device(ctx));
+    return launch_volume_mips(ctx, d_mip0, sx, sy, sz, d_mip1, d_mip2, (cudaStream_t)stream);
+}
+
+vxl_status vxl_trace_primary(vxl_ctx* ctx, const vxl_volume* volumes, int nvolumes, const vxl_voxcmd* cmds, int ncmds,
+                             const vxl_camera* cam, const vxl_primary_out* out, void* stream) {
+    if (!ctx || !cam || !out) return fail(VXL_ERR_INVALID_ARG, "trace_primary: NULL argument");
+    if (nvolumes < 0 || ncmds < 0 || (nvolumes > 0 && !volumes) || (ncmds > 0 && !cmds))
+        return fail(VXL_ERR_INVALID_ARG, "trace_primary: bad volume or command table");
+    if (cam->width < 1 || cam->height < 1 || (int64_t)cam->width * cam->height > (int64_t)INT32_MAX / 4)
+        return fail(VXL_ERR_INVALID_ARG, "trace_primary: bad image size");
+    if (!out->pos || !out->nrm) return fail(VXL_ERR_INVALID_ARG, "trace_primary: pos and nrm are required");
+    for (int v = 0; v < nvolumes; v++) {
+        const vxl_volume& V = volumes[v];
+        if (!V.mip[0] || !V.mip[1] || !V.mip[2] || V.sx < 4 || V.sy < 4 || V.sz < 4 || V.sx > 32768 ||
+            V.sy > 32768 || V.sz > 32768)
+            return fail(VXL_ERR_INVALID_ARG, "trace_primary: volume %d: NULL mip or size < 4", v);
+    }
+    for (int k = 0; k < ncmds; k++)
+        if (cmds[k].volume < 0 || cmds[k].volume >= nvolumes)
+            return fail(VXL_ERR_OUT_OF_RANGE, "trace_primary: command %d names volume %d", k, cmds[k].volume);
+    VXL_TRY(set_device(ctx));
+    return launch_trace_primary(ctx, volumes, nvolumes, cmds, ncmds, cam, out, (cudaStream_t)stream);
+}
+
 vxl_status vxl_scene_soft(vxl_ctx* ctx, float* d_soft, int nx, int ny, int nz, uint32_t seed, float thresh,
                           float sharpness, float freq, int ground_y, uint32_t albedo_seed, void* stream) {
     if (!ctx) return fail(VXL_ERR_INVALID_ARG, "scene_soft: NULL context");

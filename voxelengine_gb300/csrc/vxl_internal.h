@@ -79,6 +79,10 @@ vxl_status launch_scene_noise(vxl_grid* g, uint32_t seed, float thresh, float fr
 vxl_status launch_scene_boxes(vxl_grid* g, uint32_t seed, int nboxes, int smin, int smax, cudaStream_t s);
 vxl_status launch_scene_terrain(vxl_grid* g, uint32_t seed, float base, float amp, float freq, int octaves,
                                 float* d_height, cudaStream_t s);
+vxl_status launch_volume_mips(vxl_ctx* ctx, const uint8_t* mip0, int sx, int sy, int sz, uint8_t* mip1, uint8_t* mip2,
+                              cudaStream_t s);
+vxl_status launch_trace_primary(vxl_ctx* ctx, const vxl_volume* volumes, int nvol, const vxl_voxcmd* cmds, int ncmd,
+                                const vxl_camera* cam, const vxl_primary_out* out, cudaStream_t s);
 vxl_status launch_scene_soft(vxl_ctx* ctx, float* soft, int nx, int ny, int nz, uint32_t seed, float thresh,
                              float sharpness, float freq, int ground_y, uint32_t albedo_seed, cudaStream_t s);
 vxl_status launch_soft_fwd(vxl_ctx* ctx, const float* soft, int nx, int ny, int nz, const vxl_gbuffer* gb,
