@@ -497,11 +497,11 @@ def trace_primary(ctx, volset: VolumeSet, worlds, vol_of, cam, target, W, H, pos
     """vxl_trace_primary; worlds float[n, 16] column-major, vol_of int[n]; camera in world units."""
     worlds = np.ascontiguousarray(worlds, np.float32).reshape(-1, 16)
     n = worlds.shape[0]
-    cmds = (VoxCmd * max(1, n))()
-    for k in range(n):
-        cmds[k].world[:] = [float(x) for x in worlds[k]]
-        cmds[k].volume = int(vol_of[k])
-        cmds[k].palette = 0
+    rec = np.zeros(max(1, n), dtype=[("world", "<f4", (16,)), ("volume", "<i4"), ("palette", "<i4")])
+    if n:
+        rec["world"] = worlds
+        rec["volume"] = np.asarray(vol_of, np.int32)
+    cmds = rec.ctypes.data_as(C.POINTER(VoxCmd))
     c = Camera()
     c.pos[:] = [float(x) for x in cam]
     c.target[:] = [float(x) for x in target]
@@ -509,6 +509,7 @@ def trace_primary(ctx, volset: VolumeSet, worlds, vol_of, cam, target, W, H, pos
     out = PrimaryOut(_ptr(pos), _ptr(nrm), _ptr(depth), _ptr(material), _ptr(instance))
     check(lib().vxl_trace_primary(ctx.handle, volset.table, len(volset), cmds, n, C.byref(c), C.byref(out),
                                   _stream(stream)))
+    del rec
 
 
 def _models(models):

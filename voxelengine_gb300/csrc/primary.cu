@@ -71,6 +71,7 @@ struct PrimInst {
     float lc[3];   // camera in the volume's local space
     int vol;
     int tx0, ty0, tx1, ty1;  // screen tiles covered (inclusive); tx0 > tx1: none
+    float near;              // least view depth of the box's corners (a lower bound of any hit's depth)
 };
 
 struct PrimCam {
@@ -139,16 +140,16 @@ __global__ void k_prim_prep(const vxl_voxcmd* __restrict__ cmds, int n, const Vo
     const VolDev V = vols[P.vol];
     // screen rectangle of the box [0, dims] * 0.1 in world space
     float x0 = 1e30f, y0 = 1e30f, x1 = -1e30f, y1 = -1e30f;
+    float zmin = 1e30f;
     bool behind = false;
     for (int c = 0; c < 8; c++) {
         const f3 l = mk((c & 1) ? V.sx * 0.1f : 0.0f, (c & 2) ? V.sy * 0.1f : 0.0f, (c & 4) ? V.sz * 0.1f : 0.0f);
         const f3 w = add(cmul3(P.M, l), mk(P.M[9], P.M[10], P.M[11]));
         const f3 r = sub(w, C.cam);
         const float zc = dot(r, C.fwd);
-        if (!(zc > 1e-3f)) {
-            behind = true;
-            break;
-        }
+        zmin = fminf(zmin, zc);
+        if (!(zc > 1e-3f)) behind = true;
+        if (behind) continue;
         const float sx = dot(r, C.right) / (zc * C.tanh_ * C.aspect);
         const float sy = dot(r, C.upv) / (zc * C.tanh_);
         const float px = (sx + 1.0f) * 0.5f * (float)C.W;
@@ -177,6 +178,7 @@ __global__ void k_prim_prep(const vxl_voxcmd* __restrict__ cmds, int n, const Vo
     P.ty0 = ty0;
     P.tx1 = tx1;
     P.ty1 = ty1;
+    P.near = zmin;
     out[k] = P;
     if (tx0 <= tx1 && ty0 <= ty1)
         for (int ty = ty0; ty <= ty1; ty++)
@@ -243,16 +245,20 @@ __device__ __forceinline__ f3 clip_to_aabb(f3 o, f3 d, f3 size) {
     return add(o, mul(d, tmin - 0.001f));
 }
 
-// texelFetch(VOLUME_TEXTURE, p, mip).r with robust out-of-range = 0
+// texelFetch(VOLUME_TEXTURE, p, mip).r with robust out-of-range = 0 (mip
+// chosen by selects, not array indexing, so the volume stays in registers)
 __device__ __forceinline__ uint32_t vol_texel(const VolDev& V, int mip, int x, int y, int z) {
-    const int sx = V.dx[mip], sy = V.dy[mip], sz = V.dz[mip];
+    const int sx = mip == 0 ? V.dx[0] : (mip == 1 ? V.dx[1] : V.dx[2]);
+    const int sy = mip == 0 ? V.dy[0] : (mip == 1 ? V.dy[1] : V.dy[2]);
+    const int sz = mip == 0 ? V.dz[0] : (mip == 1 ? V.dz[1] : V.dz[2]);
+    const uint8_t* m = mip == 0 ? V.m[0] : (mip == 1 ? V.m[1] : V.m[2]);
     if (x < 0 || y < 0 || z < 0 || x >= sx || y >= sy || z >= sz) return 0u;
-    return __ldg(V.m[mip] + ((size_t)x + (size_t)y * sx + (size_t)z * sx * sy));
+    return __ldg(m + ((size_t)x + (size_t)y * sx + (size_t)z * sx * sy));
 }
 
 // intersectVolume, GeometryVoxel.frag:63-125 (LOD 1, MIP_COUNT 2,
 // TRANSPARENCY 1), operation for operation
-__device__ bool intersect_volume(const VolDev& V, f3 origin, f3 direction, f3 lcam, float uvx, float uvy, float resx,
+__device__ __forceinline__ bool intersect_volume(const VolDev& V, f3 origin, f3 direction, f3 lcam, float uvx, float uvy, float resx,
                                  float resy, int frame, f3* hit, f3* normal, uint32_t* material) {
     const f3 ss = mk(glsl_sign(direction.x), glsl_sign(direction.y), glsl_sign(direction.z));
     const f3 td = mk(1.0f / (direction.x * ss.x), 1.0f / (direction.y * ss.y), 1.0f / (direction.z * ss.z));
@@ -309,17 +315,23 @@ __device__ bool intersect_volume(const VolDev& V, f3 origin, f3 direction, f3 lc
     return false;
 }
 
-// one CTA per 16x16 screen tile, one thread per pixel
+// One CTA per 16x16 screen tile, one thread per pixel. The tile's instance
+// list is taken in chunks of 256, each sorted in shared memory by the
+// instances' nearest corner depth; a pixel stops scanning a chunk once that
+// depth, less a safety margin for rounding, is beyond its current hit (no
+// instance further in the chunk can be nearer).
 __global__ void __launch_bounds__(256) k_primary(const PrimInst* __restrict__ insts, const VolDev* __restrict__ vols,
                                                  PrimCam C, const int* __restrict__ offsets,
                                                  const int* __restrict__ lists, float* __restrict__ pos,
                                                  float* __restrict__ nrm, float* __restrict__ depth,
                                                  int32_t* __restrict__ material, int32_t* __restrict__ instance) {
+    __shared__ float s_near[256];
+    __shared__ int s_id[256];
     const int tile = blockIdx.x;
     const int tx = tile % C.tiles_x, ty = tile / C.tiles_x;
     const int px = tx * kPrimTile + (threadIdx.x % kPrimTile), py = ty * kPrimTile + (threadIdx.x / kPrimTile);
-    if (px >= C.W || py >= C.H) return;
-    const int i = py * C.W + px;
+    const bool live = px < C.W && py < C.H;
+    const int i = live ? py * C.W + px : 0;
     const float uvx = ((float)px + 0.5f) * 2.0f / (float)C.W - 1.0f;
     const float uvy = ((float)py + 0.5f) * 2.0f / (float)C.H - 1.0f;
     const float u = uvx * C.tanh_ * C.aspect;
@@ -330,39 +342,76 @@ __global__ void __launch_bounds__(256) k_primary(const PrimInst* __restrict__ in
     f3 bp = mk(0.0f, 0.0f, 0.0f), bn = mk(0.0f, 0.0f, 0.0f);
     uint32_t bm = 0;
     const int e0 = offsets[tile], e1 = offsets[tile + 1];
-    for (int e = e0; e < e1; e++) {
-        const int k = lists[e];
-        const PrimInst& P = insts[k];
-        const VolDev V = vols[P.vol];
-        const f3 lc = mk(P.lc[0], P.lc[1], P.lc[2]);
-        const f3 ld = normalize(rmul3(P.ri, d));
-        // the pixel ray enters the volume box
-        const float dims[3] = {(float)V.sx, (float)V.sy, (float)V.sz};
-        const float lo[3] = {lc.x, lc.y, lc.z}, dl[3] = {ld.x, ld.y, ld.z};
-        float t0 = -INFINITY, t1 = INFINITY;
-#pragma unroll
-        for (int a = 0; a < 3; a++) {
-            const float inv = 1.0f / dl[a];
-            const float ta = (0.0f - lo[a]) * inv, tb = (dims[a] - lo[a]) * inv;
-            t0 = fmaxf(t0, fminf(ta, tb));
-            t1 = fminf(t1, fmaxf(ta, tb));
+    for (int c0 = e0; c0 < e1; c0 += 256) {
+        const int cn = min(256, e1 - c0);
+        __syncthreads();
+        if ((int)threadIdx.x < cn) {
+            const int k = lists[c0 + threadIdx.x];
+            s_id[threadIdx.x] = k;
+            s_near[threadIdx.x] = insts[k].near;
+        } else {
+            s_id[threadIdx.x] = 0x7fffffff;
+            s_near[threadIdx.x] = INFINITY;
         }
-        if (!(t0 <= t1 && t1 >= 0.0f)) continue;
-        const f3 o = clip_to_aabb(lc, ld, mk(dims[0], dims[1], dims[2]));
-        f3 h, nn;
-        uint32_t mat;
-        if (!intersect_volume(V, o, ld, lc, uvx, uvy, (float)C.W, (float)C.H, C.frame, &h, &nn, &mat)) continue;
-        const f3 wl = cmul3(P.M, mul(h, 0.1f));
-        const f3 wp = mk(wl.x + P.M[9], wl.y + P.M[10], wl.z + P.M[11]);
-        const float dep = dot(sub(wp, C.cam), C.fwd);
-        if (bi < 0 || dep < best || (dep == best && k < bi)) {
-            best = dep;
-            bi = k;
-            bp = wp;
-            bn = nn;
-            bm = mat;
+        __syncthreads();
+        // bitonic sort of the 256 (near, id) pairs, ascending
+        for (int size = 2; size <= 256; size <<= 1)
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                const int a = threadIdx.x, b = a ^ stride;
+                if (b > a) {
+                    const bool up = (a & size) == 0;
+                    const float na = s_near[a], nb = s_near[b];
+                    const int ia = s_id[a], ib = s_id[b];
+                    const bool gt = na > nb || (na == nb && ia > ib);
+                    if (gt == up) {
+                        s_near[a] = nb;
+                        s_near[b] = na;
+                        s_id[a] = ib;
+                        s_id[b] = ia;
+                    }
+                }
+                __syncthreads();
+            }
+        if (live) {
+            for (int e = 0; e < cn; e++) {
+                const float nz = s_near[e];
+                if (bi >= 0 && nz - (1e-3f * fabsf(nz) + 1e-3f) > best) break;
+                const int k = s_id[e];
+                const PrimInst& P = insts[k];
+                const VolDev V = vols[P.vol];
+                const f3 lc = mk(P.lc[0], P.lc[1], P.lc[2]);
+                const f3 ld = normalize(rmul3(P.ri, d));
+                // the pixel ray enters the volume box
+                const float dims[3] = {(float)V.sx, (float)V.sy, (float)V.sz};
+                const float lo[3] = {lc.x, lc.y, lc.z}, dl[3] = {ld.x, ld.y, ld.z};
+                float t0 = -INFINITY, t1 = INFINITY;
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    const float inv = 1.0f / dl[a];
+                    const float ta = (0.0f - lo[a]) * inv, tb = (dims[a] - lo[a]) * inv;
+                    t0 = fmaxf(t0, fminf(ta, tb));
+                    t1 = fminf(t1, fmaxf(ta, tb));
+                }
+                if (!(t0 <= t1 && t1 >= 0.0f)) continue;
+                const f3 o = clip_to_aabb(lc, ld, mk(dims[0], dims[1], dims[2]));
+                f3 h, nn;
+                uint32_t mat;
+                if (!intersect_volume(V, o, ld, lc, uvx, uvy, (float)C.W, (float)C.H, C.frame, &h, &nn, &mat))
+                    continue;
+                const f3 wl = cmul3(P.M, mul(h, 0.1f));
+                const f3 wp = mk(wl.x + P.M[9], wl.y + P.M[10], wl.z + P.M[11]);
+                const float dep = dot(sub(wp, C.cam), C.fwd);
+                if (bi < 0 || dep < best || (dep == best && k < bi)) {
+                    best = dep;
+                    bi = k;
+                    bp = wp;
+                    bn = nn;
+                    bm = mat;
+                }
+            }
         }
     }
+    if (!live) return;
     float* po = pos + 3 * (size_t)i;
     float* no = nrm + 3 * (size_t)i;
     if (bi >= 0) {
