@@ -415,6 +415,45 @@ typedef struct vxl_primary_out {
 vxl_status vxl_trace_primary(vxl_ctx* ctx, const vxl_volume* volumes, int nvolumes, const vxl_voxcmd* cmds, int ncmds,
                              const vxl_camera* camera, const vxl_primary_out* out, void* stream);
 
+/* ---------------------------------------------------------- scene assets
+ * Host-side readers for the reference's shipped scenes (no device work). */
+/* Asset GUID of a mod-relative path such as "default/FarmHouse/0.v":
+ * Assets::Hash (Assets.h:207-210), std::hash<std::string> as the shipped
+ * files were written with it (MSVC: FNV-1a 64). */
+uint64_t vxl_asset_guid(const char* mod_path);
+/* .p palette (PalleteAsset::Serialize, PalleteAsset.h:63-69): 256 VoxMaterial
+ * of 7 bytes (r, g, b, a, roughness, metallic, emit) into h_materials[1792]. */
+vxl_status vxl_read_palette(const char* path, uint8_t* h_materials);
+/* TransformSystem::RealculateMatrix (TransformSystem.cpp:124-135):
+ * out = parent * T(pos) Rz(rot.z) Ry(rot.y) Rx(rot.x) S(scale), column-major,
+ * radians; parent NULL = identity. glm's operation order, C library cos/sin. */
+vxl_status vxl_transform_matrix(const float pos[3], const float rot[3], const float scale[3], const float* parent,
+                                float out[16]);
+/* A spawned .pf prefab (PrefabAsset::Spawn, PrefabAsset.cpp:30-120) without a
+ * world: mods_dir holds the mod folders ("Assets/Mods"), mod_path names the
+ * prefab ("default/FarmHouse.pf"). GUIDs resolve to files under mods_dir by
+ * vxl_asset_guid of their mod-relative paths; nested prefab instances spawn
+ * under the instance entity's parent and take its components. Each entity
+ * with a VoxRenderer whose Vox GUID is not null gives one renderer, in
+ * creation order; volumes and palettes are listed once each, in order of
+ * first use. A non-null GUID that resolves to no file is an error. */
+typedef struct vxl_prefab vxl_prefab;
+typedef struct vxl_prefab_renderer {
+    float world[16];   /* the entity's WorldMatrix; voxelize / draw with world * translate(-pivot) */
+    float pivot[3];
+    int32_t volume;    /* index into the prefab's volumes */
+    int32_t palette;   /* index into the prefab's palettes */
+    int32_t entity;    /* creation order of the entity */
+} vxl_prefab_renderer;
+vxl_status vxl_prefab_load(const char* mods_dir, const char* mod_path, vxl_prefab** out);
+vxl_status vxl_prefab_info(const vxl_prefab* prefab, int32_t* n_renderers, int32_t* n_volumes, int32_t* n_palettes);
+vxl_status vxl_prefab_renderer_at(const vxl_prefab* prefab, int i, vxl_prefab_renderer* out);
+/* volume i: sizes, host data (owned by the prefab, [sz][sy][sx]) and GUID */
+vxl_status vxl_prefab_volume_at(const vxl_prefab* prefab, int i, int32_t* sx, int32_t* sy, int32_t* sz,
+                                const uint8_t** h_data, uint64_t* guid);
+vxl_status vxl_prefab_palette_at(const vxl_prefab* prefab, int i, const uint8_t** h_materials, uint64_t* guid);
+vxl_status vxl_prefab_destroy(vxl_prefab* prefab);
+
 /* .v asset reader (VoxAsset::Serialize, VoxAsset.h:42-50): u32 sx,sy,sz then
  * sx*sy*sz bytes. Query with data == NULL to get the sizes, then read into a
  * host buffer of sx*sy*sz bytes. */

@@ -21,6 +21,9 @@ output into oracle/_ref/ (git-ignored):
   (same two edits, plus `out uint` -> `uint&`) and compiled inside
   ref_geometry_harness.cpp with a three-mip R8 volume; the mip loop of
   VoxAsset::Upload (Sources/Asset/VoxAsset.cpp) is cut out and compiled there too.
+* TransformSystem::RealculateMatrix (Sources/World/Systems/TransformSystem.cpp)
+  is cut out, made a free function, and compiled in ref_transform_harness.cpp
+  against the vendored glm.
 
 Compiler flags: -O2 -ffp-contract=off -fsingle-precision-constant (GLSL float
 literals are single precision). Output: oracle/_ref/libvxl_ref.so.
@@ -104,10 +107,13 @@ def generate() -> None:
     spot = open(os.path.join(sh, "LightSpot.frag")).read()
     geo = open(os.path.join(sh, "GeometryVoxel.frag")).read()
     voxasset = open(os.path.join(r, "Sources", "Asset", "VoxAsset.cpp")).read()
+    transform = open(os.path.join(r, "Sources", "World", "Systems", "TransformSystem.cpp")).read()
     parts = {
         "geometry_clip.inc": _glslpp(_function(geo, "vec3 clipToAABB(")),
         "geometry_intersect.inc": _glslpp(_function(geo, "bool intersectVolume(")),
         "voxasset_mip.inc": _braced_from(voxasset, "for (int x = 0; x < mipSizeX; x++)"),
+        "transform_realculate.inc": _function(transform, "void TransformSystem::RealculateMatrix(").replace(
+            "TransformSystem::", "", 1),
         "Light_frag.inc": _glslpp(light),
         "ambient_cosine.inc": _glslpp(_function(amb, "vec3 cosineSampleHemisphere(")),
         "ambient_irradiance.inc": _glslpp(_function(amb, "vec3 calculateAmbientIrradiance(")),
@@ -134,7 +140,7 @@ def build(force: bool = False, verbose: bool = False) -> str | None:
     if not available():
         return None
     srcs = [os.path.join(HERE, "ref_light_harness.cpp"), os.path.join(HERE, "ref_voxelizer_harness.cpp"),
-            os.path.join(HERE, "ref_geometry_harness.cpp")]
+            os.path.join(HERE, "ref_geometry_harness.cpp"), os.path.join(HERE, "ref_transform_harness.cpp")]
     if not force and os.path.exists(SO) and os.path.getmtime(SO) >= max(os.path.getmtime(s) for s in srcs + [__file__]):
         return SO
     generate()
@@ -161,6 +167,10 @@ def build(force: bool = False, verbose: bool = False) -> str | None:
     o4 = os.path.join(OUT, "ref_geometry.o")
     subprocess.run(common + ["-c", "-I", OUT, "-I", os.path.join(r, "Vendor"), srcs[2], "-o", o4], check=True)
     objs.append(o4)
+    # TransformSystem::RealculateMatrix (no -fsingle-precision-constant needed: C++ source)
+    o5 = os.path.join(OUT, "ref_transform.o")
+    subprocess.run(common + ["-c", "-I", OUT, "-I", os.path.join(r, "Vendor"), srcs[3], "-o", o5], check=True)
+    objs.append(o5)
     tmp = SO + ".tmp%d" % os.getpid()
     subprocess.run(["g++", "-shared", "-o", tmp] + objs, check=True)
     os.replace(tmp, SO)

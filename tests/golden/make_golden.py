@@ -116,6 +116,36 @@ def main():
                         ent_model=np.array([e[0] for e in ents], np.int32), prev=np.stack([e[1] for e in ents]),
                         cur=np.stack([e[2] for e in ents]), pivot=np.stack([e[3] for e in ents]),
                         regions=out[:nreg], nz_index=nz, nz_value=buf[nz])
+    # ---- the shipped FarmHouse prefab as world-space placements (PrefabAsset::Spawn
+    # + TransformSystem::RealculateMatrix of the reference, then World * translate(-Pivot))
+    mods = os.path.join(build_ref.reference_dir(), "Assets", "Mods")
+    if os.path.isdir(mods):
+        from tests import prefab_walk
+
+        R.ref_transform.argtypes = [fp, fp, fp, fp, fp]
+
+        def realculate(pos, rot, scale, parent=None):
+            o = np.zeros(16, np.float32)
+            par = None if parent is None else np.ascontiguousarray(parent, np.float32)
+            R.ref_transform(f(pos), f(rot), f(scale), None if par is None else f(par), o.ctypes.data_as(fp))
+            return o
+
+        rens = prefab_walk.spawn(mods, "default/FarmHouse.pf", realculate)
+        guids = []
+        for _, _, vg, _, _ in rens:
+            if vg not in guids:
+                guids.append(vg)
+        idx = rens[0][4]
+        vols = [vox_cases.read_v(idx[g]) for g in guids]
+        worlds = np.stack([r[0] for r in rens])
+        pivots = np.stack([r[1] for r in rens])
+        mats = np.stack([oracle.translate(w, -p) for w, p in zip(worlds, pivots)])
+        pal = np.frombuffer(open(idx[rens[0][3]], "rb").read(), np.uint8)
+        np.savez_compressed(os.path.join(HERE, "farmhouse_scene.npz"),
+                            volumes=np.concatenate([v.reshape(-1) for v in vols]),
+                            volume_shapes=np.array([v.shape for v in vols], np.int32),
+                            vol_of=np.array([guids.index(r[2]) for r in rens], np.int32), world=worlds,
+                            pivot=pivots, matrix=mats, palette=pal)
     print("golden fixtures written to", HERE)
 
 

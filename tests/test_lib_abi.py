@@ -13,7 +13,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def declared_functions():
     src = open(os.path.join(ROOT, "include", "vxl.h")).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"^\s*(?:vxl_status|int|const char\*)\s+(vxl_\w+)\s*\(", src, flags=re.M)))
+    return sorted(set(re.findall(r"^\s*(?:vxl_status|int|uint64_t|const char\*)\s+(vxl_\w+)\s*\(", src, flags=re.M)))
 
 
 @pytest.fixture(scope="module")

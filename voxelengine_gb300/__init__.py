@@ -41,6 +41,8 @@ EXPORTED = [
     "vxl_light_reflection", "vxl_light_point", "vxl_voxelize", "vxl_voxelize_noalloc", "vxl_shadowvox_update",
     "vxl_vox_destroyed",
     "vxl_trace_soft_fwd", "vxl_trace_soft_bwd", "vxl_volume_build_mips", "vxl_trace_primary",
+    "vxl_asset_guid", "vxl_read_palette", "vxl_transform_matrix", "vxl_prefab_load", "vxl_prefab_info",
+    "vxl_prefab_renderer_at", "vxl_prefab_volume_at", "vxl_prefab_palette_at", "vxl_prefab_destroy",
     "vxl_read_v", "vxl_scene_soft", "vxl_scene_terrain", "vxl_scene_noise", "vxl_scene_boxes", "vxl_scene_gbuffer",
 ]
 
@@ -108,6 +110,11 @@ class Camera(C.Structure):
 class PrimaryOut(C.Structure):
     _fields_ = [("pos", C.c_void_p), ("nrm", C.c_void_p), ("depth", C.c_void_p), ("material", C.c_void_p),
                 ("instance", C.c_void_p)]
+
+
+class PrefabRenderer(C.Structure):
+    _fields_ = [("world", C.c_float * 16), ("pivot", C.c_float * 3), ("volume", C.c_int32), ("palette", C.c_int32),
+                ("entity", C.c_int32)]
 
 
 class Model(C.Structure):
@@ -178,6 +185,18 @@ def lib():
         L.vxl_vox_destroyed.argtypes = [vp, vp, C.POINTER(Model), C.POINTER(f * 16), vp, vp]
         L.vxl_read_v.argtypes = [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), vp,
                                  C.c_size_t]
+        L.vxl_asset_guid.restype = C.c_uint64
+        L.vxl_asset_guid.argtypes = [C.c_char_p]
+        L.vxl_read_palette.argtypes = [C.c_char_p, vp]
+        L.vxl_transform_matrix.argtypes = [vp, vp, vp, vp, vp]
+        L.vxl_prefab_load.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(vp)]
+        L.vxl_prefab_info.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+        L.vxl_prefab_renderer_at.argtypes = [vp, C.c_int, C.POINTER(PrefabRenderer)]
+        L.vxl_prefab_volume_at.argtypes = [vp, C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                           C.POINTER(C.c_int32), C.POINTER(C.POINTER(C.c_uint8)),
+                                           C.POINTER(C.c_uint64)]
+        L.vxl_prefab_palette_at.argtypes = [vp, C.c_int, C.POINTER(C.POINTER(C.c_uint8)), C.POINTER(C.c_uint64)]
+        L.vxl_prefab_destroy.argtypes = [vp]
         L.vxl_volume_build_mips.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp]
         L.vxl_trace_primary.argtypes = [vp, C.POINTER(Volume), C.c_int, C.POINTER(VoxCmd), C.c_int, C.POINTER(Camera),
                                         C.POINTER(PrimaryOut), vp]
@@ -192,7 +211,7 @@ def lib():
         L.vxl_scene_gbuffer.argtypes = [vp, vp, C.POINTER(f * 3), C.POINTER(f * 3), f, C.c_int, C.c_int, C.c_uint32,
                                         vp, vp, vp, vp]
         for name in EXPORTED:
-            if name not in ("vxl_abi_version", "vxl_last_error_string", "vxl_status_string"):
+            if name not in ("vxl_abi_version", "vxl_last_error_string", "vxl_status_string", "vxl_asset_guid"):
                 getattr(L, name).restype = C.c_int
         _lib = L
         return L
@@ -564,6 +583,61 @@ def vox_destroyed(ctx, grid, model, world, stream=None):
     region = np.zeros(6, np.int32)
     check(lib().vxl_vox_destroyed(ctx.handle, grid.handle, ms, C.byref(w), _ptr(region), _stream(stream)))
     return region
+
+
+def asset_guid(mod_path: str) -> int:
+    return lib().vxl_asset_guid(mod_path.encode())
+
+
+def read_palette(path: str) -> np.ndarray:
+    out = np.zeros((256, 7), np.uint8)
+    check(lib().vxl_read_palette(path.encode(), out.ctypes.data))
+    return out
+
+
+def transform_matrix(pos, rot, scale, parent=None) -> np.ndarray:
+    p = np.asarray(pos, np.float32)
+    r = np.asarray(rot, np.float32)
+    s_ = np.asarray(scale, np.float32)
+    par = None if parent is None else np.ascontiguousarray(parent, np.float32).reshape(16)
+    out = np.zeros(16, np.float32)
+    check(lib().vxl_transform_matrix(p.ctypes.data, r.ctypes.data, s_.ctypes.data,
+                                     None if par is None else par.ctypes.data, out.ctypes.data))
+    return out
+
+
+def load_prefab(mods_dir: str, mod_path: str) -> dict:
+    """vxl_prefab_load: returns dict(renderers=[(world16, pivot3, volume, palette, entity)],
+    volumes=[uint8 [sz, sy, sx]], palettes=[uint8 [256, 7]], volume_guids, palette_guids)."""
+    h = C.c_void_p()
+    check(lib().vxl_prefab_load(mods_dir.encode(), mod_path.encode(), C.byref(h)))
+    try:
+        nr, nv, npal = C.c_int32(), C.c_int32(), C.c_int32()
+        check(lib().vxl_prefab_info(h, C.byref(nr), C.byref(nv), C.byref(npal)))
+        rens = []
+        for i in range(nr.value):
+            r = PrefabRenderer()
+            check(lib().vxl_prefab_renderer_at(h, i, C.byref(r)))
+            rens.append((np.array(r.world, np.float32), np.array(r.pivot, np.float32), r.volume, r.palette, r.entity))
+        vols, vg = [], []
+        for i in range(nv.value):
+            sx, sy, sz = C.c_int32(), C.c_int32(), C.c_int32()
+            ptr = C.POINTER(C.c_uint8)()
+            g = C.c_uint64()
+            check(lib().vxl_prefab_volume_at(h, i, C.byref(sx), C.byref(sy), C.byref(sz), C.byref(ptr), C.byref(g)))
+            n = sx.value * sy.value * sz.value
+            vols.append(np.ctypeslib.as_array(ptr, (n,)).copy().reshape(sz.value, sy.value, sx.value))
+            vg.append(g.value)
+        pals, pg = [], []
+        for i in range(npal.value):
+            ptr = C.POINTER(C.c_uint8)()
+            g = C.c_uint64()
+            check(lib().vxl_prefab_palette_at(h, i, C.byref(ptr), C.byref(g)))
+            pals.append(np.ctypeslib.as_array(ptr, (256 * 7,)).copy().reshape(256, 7))
+            pg.append(g.value)
+        return dict(renderers=rens, volumes=vols, palettes=pals, volume_guids=vg, palette_guids=pg)
+    finally:
+        lib().vxl_prefab_destroy(h)
 
 
 def read_v(path: str) -> np.ndarray:
