@@ -647,13 +647,28 @@ def run_gpu_frame(args):
         torch.cuda.synchronize()
         return sum(a.elapsed_time(b) for a, b in ts) / 1e3 / args.steps
 
+    # 64 point / spot lights over the scene (every third a spot), shadows fused in one launch
+    lrng = np.random.default_rng(seed + 1)
+    lights = [(lrng.uniform(0.0, n / 10.0, 3).astype(np.float32), float(lrng.uniform(4.0, 12.0)), l % 3 == 2)
+              for l in range(64)]
+    wpos = torch.empty_like(pos)
+    noise = torch.rand(npix * 4, dtype=torch.float32, device="cuda")
+    lit = torch.empty(npix, dtype=torch.int64, device="cuda")
+    inr = torch.empty_like(lit)
+
+    def lights_pass():
+        torch.mul(pos, 0.1, out=wpos)
+        V.light_points(ctx, G, wpos, nrm, noise, npix, lights, lit, inr)
+
     primary()
     torch.cuda.synchronize()
     valid = int((nrm.view(-1, 3).abs().sum(1) > 0).sum().item())
     with ClockSampler(0) as clk:
         t_p = timed(primary)
         t_o = timed(occl)
+        t_l = timed(lights_pass)
         t_f = timed(lambda: (primary(), occl()))
+    pairs = int(sum(bin(int(x)).count("1") for x in inr.cpu().numpy().view(np.uint64)))
     line = {
         "metric": "frame ms: primary visibility + shadow/AO/spec occlusion, 4096 instances, 1080p",
         "value": t_f * 1e3, "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -663,6 +678,7 @@ def run_gpu_frame(args):
                    "model_edges": [16, 64], "l2": "flushed between timed steps"},
         "primary_ms": t_p * 1e3, "primary_mpix_per_s": npix / t_p / 1e6, "occlusion_ms": t_o * 1e3,
         "occlusion_grays_per_s": valid * 10 / t_o / 1e9, "covered_pixels": valid,
+        "lights64_ms": t_l * 1e3, "light_rays": pairs, "light_grays_per_s": pairs / t_l / 1e9,
         "voxelize": {"seconds": t_vox, "instances": ninst}, "clocks": clk.summary(),
     }
     if not args.no_cpu_baseline:

@@ -243,6 +243,23 @@ vxl_status vxl_light_point(vxl_ctx* ctx, const vxl_grid* grid, const float* d_wp
                            const float* d_noise, int64_t npix, const float light_pos[3], float range, int spot,
                            float* d_shadow, vxl_ray_record* d_records, void* stream);
 
+/* Fused point / spot shadows for up to 64 lights (the per-light passes of
+ * LightPointPipeline / LightSpotPipeline, LightPoint.frag:94-129,
+ * LightSpot.frag:83-117, in one launch). For pixel i and light l: in range
+ * when |light.pos - wpos| <= range (the pass's discard test); then the same
+ * jittered shadow ray vxl_light_point traces for that light. Out (device
+ * uint64 per pixel): bit l of d_lit = in range and unshadowed; bit l of
+ * d_in_range (optional) = in range. Host light table. */
+typedef struct vxl_light {
+    float pos[3];      /* world units */
+    float range;
+    int32_t spot;      /* 0: point light (Sparse marcher), 1: spot light (SuperSparse marcher) */
+    int32_t pad[3];
+} vxl_light;
+vxl_status vxl_light_points(vxl_ctx* ctx, const vxl_grid* grid, const float* d_wpos, const float* d_nrm,
+                            const float* d_noise, int64_t npix, const vxl_light* lights, int nlights,
+                            uint64_t* d_lit, uint64_t* d_in_range, void* stream);
+
 /* ------------------------------------------------------------ voxelizer */
 typedef struct vxl_model {
     const uint8_t* data;   /* device palette indices [sz][sy][sx] (VoxAsset::PixelAt, VoxAsset.h:52-56) */

@@ -201,3 +201,37 @@ def test_light_passes_bit_exact(vxl, ctx, g64):
         torch.cuda.synchronize()
         assert np.array_equal(d_s.cpu().numpy(), want), spot
         assert_recs_equal(recs_np(d_rec3), r_pt, "point/spot")
+
+
+def test_light_points_fused_matches_per_light(vxl, ctx, g64):
+    """vxl_light_points (64 point and spot lights in one launch) against the
+    oracle's per-light pass: bit l of the masks = in range / in range and lit."""
+    import torch
+
+    G = grid_from_r8(vxl, ctx, g64)
+    rng = np.random.default_rng(17)
+    n = 12000
+    axes = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1]], np.float32)
+    wpos = rng.uniform(0.2, 6.2, (n, 3)).astype(np.float32)
+    nrm = axes[rng.integers(0, 6, n)]
+    noise = rng.random((n, 4)).astype(np.float32)
+    lights = [(rng.uniform(0.5, 6.0, 3).astype(np.float32), float(rng.uniform(0.8, 4.0)), bool(l % 3 == 2))
+              for l in range(64)]
+    lit = torch.full((n,), -1, dtype=torch.int64, device="cuda")
+    inr = torch.full((n,), -1, dtype=torch.int64, device="cuda")
+    vxl.light_points(ctx, G, dev(wpos), dev(nrm), dev(noise), n, lights, lit, inr)
+    torch.cuda.synchronize()
+    got_lit = lit.cpu().numpy().view(np.uint64)
+    got_in = inr.cpu().numpy().view(np.uint64)
+    want_lit = np.zeros(n, np.uint64)
+    want_in = np.zeros(n, np.uint64)
+    for l, (lp, r, spot) in enumerate(lights):
+        sh, _ = oracle.light_point(g64, wpos, nrm, noise, lp, r, spot=spot, init=np.full(n, -7.0, np.float32))
+        b = np.uint64(1) << np.uint64(l)
+        want_in |= np.where(sh != -7.0, b, np.uint64(0))
+        want_lit |= np.where(sh == 1.0, b, np.uint64(0))
+    assert np.array_equal(got_in, want_in)
+    assert np.array_equal(got_lit, want_lit)
+    assert (want_in != 0).mean() > 0.5 and (want_in != want_lit).any()
+    with pytest.raises(vxl.VxlError):
+        vxl.light_points(ctx, G, dev(wpos), dev(nrm), dev(noise), n, lights + lights[:1], lit)

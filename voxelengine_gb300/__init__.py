@@ -38,7 +38,7 @@ EXPORTED = [
     "vxl_grid_build_bricks", "vxl_grid_import_r8", "vxl_grid_export_r8", "vxl_grid_import_palette",
     "vxl_grid_count", "vxl_trace_rays", "vxl_trace_occlusion", "vxl_trace_occlusion_host", "vxl_batch_create",
     "vxl_batch_run", "vxl_batch_destroy", "vxl_batch_info", "vxl_light_ambient",
-    "vxl_light_reflection", "vxl_light_point", "vxl_voxelize", "vxl_voxelize_noalloc", "vxl_shadowvox_update",
+    "vxl_light_reflection", "vxl_light_point", "vxl_light_points", "vxl_voxelize", "vxl_voxelize_noalloc", "vxl_shadowvox_update",
     "vxl_vox_destroyed",
     "vxl_trace_soft_fwd", "vxl_trace_soft_bwd", "vxl_volume_build_mips", "vxl_trace_primary",
     "vxl_asset_guid", "vxl_read_palette", "vxl_transform_matrix", "vxl_prefab_load", "vxl_prefab_info",
@@ -112,6 +112,10 @@ class PrimaryOut(C.Structure):
                 ("instance", C.c_void_p)]
 
 
+class Light(C.Structure):
+    _fields_ = [("pos", C.c_float * 3), ("range", C.c_float), ("spot", C.c_int32), ("pad", C.c_int32 * 3)]
+
+
 class PrefabRenderer(C.Structure):
     _fields_ = [("world", C.c_float * 16), ("pivot", C.c_float * 3), ("volume", C.c_int32), ("palette", C.c_int32),
                 ("entity", C.c_int32)]
@@ -178,6 +182,7 @@ def lib():
         L.vxl_light_ambient.argtypes = [vp, vp, vp, vp, vp, vp, i64, vp, vp, vp, vp]
         L.vxl_light_reflection.argtypes = [vp, vp, vp, vp, vp, vp, vp, i64, vp, vp, vp]
         L.vxl_light_point.argtypes = [vp, vp, vp, vp, vp, i64, C.POINTER(f * 3), f, C.c_int, vp, vp, vp]
+        L.vxl_light_points.argtypes = [vp, vp, vp, vp, vp, i64, C.POINTER(Light), C.c_int, vp, vp, vp]
         L.vxl_voxelize.argtypes = [vp, vp, C.POINTER(Model), C.c_int, C.POINTER(Instance), C.c_int, vp, vp]
         L.vxl_voxelize_noalloc.argtypes = [C.POINTER(GridDesc), C.POINTER(Model), C.c_int, C.POINTER(Instance),
                                            C.c_int, vp, vp]
@@ -434,6 +439,17 @@ def light_point(ctx, grid, wpos, nrm, noise, npix, light_pos, light_range, spot,
     check(lib().vxl_light_point(ctx.handle, grid.handle, _ptr(wpos), _ptr(nrm), _ptr(noise), npix,
                                 C.byref(_f3(light_pos)), float(light_range), 1 if spot else 0, _ptr(shadow),
                                 _ptr(records), _stream(stream)))
+
+
+def light_points(ctx, grid, wpos, nrm, noise, npix, lights, lit, in_range=None, stream=None):
+    """lights: list of (pos3, range, spot)."""
+    arr = (Light * max(1, len(lights)))()
+    for i, (p, r, sp) in enumerate(lights):
+        arr[i].pos[:] = [float(x) for x in p]
+        arr[i].range = float(r)
+        arr[i].spot = 1 if sp else 0
+    check(lib().vxl_light_points(ctx.handle, grid.handle, _ptr(wpos), _ptr(nrm), _ptr(noise), npix, arr, len(lights),
+                                 _ptr(lit), _ptr(in_range), _stream(stream)))
 
 
 def scene_gbuffer(ctx, grid, cam, target, W, H, seed, d_pos, d_nrm, d_rough, tan_half_fov=0.57735026, stream=None):

@@ -207,6 +207,50 @@ __global__ void k_light_point(GridView g, const float* __restrict__ wpos, const 
     }
 }
 
+// Fused point / spot shadows: threads over (pixel, light) with the light as
+// blockIdx.y, so a warp traces one light's rays from 32 neighbouring pixels.
+// The ray of each pair is the one k_light_point traces for that light alone;
+// the results are OR-ed into per-pixel 64-bit masks.
+struct LightDev {
+    f3 pos;
+    float range;
+    int spot;
+};
+__global__ void k_light_points(GridView g, const float* __restrict__ wpos, const float* __restrict__ nrm,
+                               const float4* __restrict__ noise, int64_t npix, const LightDev* __restrict__ lights,
+                               unsigned long long* __restrict__ lit, unsigned long long* __restrict__ in_range) {
+    const int l = blockIdx.y;
+    const LightDev Lt = lights[l];
+    const unsigned long long bit = 1ull << l;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npix;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const f3 worldPos = ld3(wpos + 3 * i);
+        const f3 lightDir = sub(Lt.pos, worldPos);
+        const float lightDistance = sqrtf(dot(lightDir, lightDir));
+        if (lightDistance > Lt.range) continue;  // the light's pass discards this pixel
+        const float4 nz = noise[i];
+        const f3 normal = ld3(nrm + 3 * i);
+        f3 wd;
+        float hitDist;
+        if (Lt.spot) {
+            wd = mul(normalize(lightDir), 10.0f);
+            hitDist = lightDistance * 10.0f;
+        } else {
+            wd = lightDir;
+            hitDist = lightDistance * 10.5f;
+        }
+        f3 wcp = mul(worldPos, 10.0f);
+        f3 randomVec = mul(cosine_sample(nz.x, nz.y), 0.1f);
+        randomVec.z *= glsl_sign(nz.z - 0.5f);
+        wd = normalize(mix(wd, randomVec, 0.5f));
+        wcp = add(wcp, mul(wd, nz.w * 1.0f));
+        wcp = add(wcp, mul(randomVec, 2.5f));
+        const Hit h = march(g, add(wcp, mul(normal, 0.5f)), wd, hitDist, Lt.spot ? 2.5f : 0.5f);
+        if (in_range) atomicOr(in_range + i, bit);
+        if (!(h.t < hitDist)) atomicOr(lit + i, bit);
+    }
+}
+
 // ---------------------------------------------------------------- launchers
 static unsigned grid_blocks(vxl_ctx* ctx, int64_t n, int threads, int per_sm) {
     int64_t need = (n + threads - 1) / threads;
@@ -302,6 +346,32 @@ vxl_status launch_light_point(vxl_ctx* ctx, const vxl_grid* g, const float* wpos
     GridView v = view_of(g);
     k_light_point<<<grid_blocks(ctx, npix, 128, 16), 128, 0, s>>>(v, wpos, nrm, (const float4*)noise, npix,
                                                                   mk(lp[0], lp[1], lp[2]), range, spot, shadow, rec);
+    ctx->launches++;
+    VXL_TRY_CUDA(cudaGetLastError());
+    return VXL_OK;
+}
+
+vxl_status launch_light_points(vxl_ctx* ctx, const vxl_grid* g, const float* wpos, const float* nrm,
+                               const float* noise, int64_t npix, const vxl_light* lights, int nlights,
+                               unsigned long long* lit, unsigned long long* in_range, cudaStream_t s) {
+    VXL_TRY_CUDA(cudaMemsetAsync(lit, 0, sizeof(unsigned long long) * (size_t)npix, s));
+    if (in_range) VXL_TRY_CUDA(cudaMemsetAsync(in_range, 0, sizeof(unsigned long long) * (size_t)npix, s));
+    if (npix <= 0 || nlights <= 0) return VXL_OK;
+    LightDev h[64];
+    for (int l = 0; l < nlights; l++) {
+        h[l].pos = mk(lights[l].pos[0], lights[l].pos[1], lights[l].pos[2]);
+        h[l].range = lights[l].range;
+        h[l].spot = lights[l].spot ? 1 : 0;
+    }
+    void* p;
+    VXL_TRY(ctx_scratch(ctx, sizeof(LightDev) * 64, &p));
+    VXL_TRY_CUDA(cudaMemcpyAsync(p, h, sizeof(LightDev) * (size_t)nlights, cudaMemcpyHostToDevice, s));
+    GridView v = view_of(g);
+    int64_t bx = (npix + 127) / 128;
+    const int64_t cap = (int64_t)ctx->sm_count * 16 * 4 / nlights + 1;
+    if (bx > cap) bx = cap;
+    dim3 grid((unsigned)bx, (unsigned)nlights);
+    k_light_points<<<grid, 128, 0, s>>>(v, wpos, nrm, (const float4*)noise, npix, (const LightDev*)p, lit, in_range);
     ctx->launches++;
     VXL_TRY_CUDA(cudaGetLastError());
     return VXL_OK;

@@ -572,6 +572,23 @@ vxl_status vxl_light_point(vxl_ctx* ctx, const vxl_grid* g, const float* d_wpos,
                               d_records, (cudaStream_t)stream);
 }
 
+vxl_status vxl_light_points(vxl_ctx* ctx, const vxl_grid* g, const float* d_wpos, const float* d_nrm,
+                            const float* d_noise, int64_t npix, const vxl_light* lights, int nlights,
+                            uint64_t* d_lit, uint64_t* d_in_range, void* stream) {
+    if (!ctx || !grid_ok(g) || npix < 0 || nlights < 0 || nlights > 64 || (nlights > 0 && !lights))
+        return fail(VXL_ERR_INVALID_ARG, "light_points: bad argument (at most 64 lights)");
+    if (npix > 0 && (!d_wpos || !d_nrm || !d_noise || !d_lit))
+        return fail(VXL_ERR_INVALID_ARG, "light_points: NULL buffer");
+    for (int l = 0; l < nlights; l++)
+        if (!std::isfinite(lights[l].range) || !std::isfinite(lights[l].pos[0]) || !std::isfinite(lights[l].pos[1]) ||
+            !std::isfinite(lights[l].pos[2]))
+            return fail(VXL_ERR_INVALID_ARG, "light_points: light %d is not finite", l);
+    VXL_TRY(set_device(ctx));
+    return launch_light_points(ctx, g, d_wpos, d_nrm, d_noise, npix, lights, nlights,
+                               reinterpret_cast<unsigned long long*>(d_lit),
+                               reinterpret_cast<unsigned long long*>(d_in_range), (cudaStream_t)stream);
+}
+
 vxl_status vxl_voxelize(vxl_ctx* ctx, vxl_grid* g, const vxl_model* models, int nmodels,
                         const vxl_instance* instances, int n, int32_t* d_aabb, void* stream) {
     if (!ctx || !grid_ok(g) || n < 0 || (n > 0 && !instances)) return fail(VXL_ERR_INVALID_ARG, "voxelize: bad argument");

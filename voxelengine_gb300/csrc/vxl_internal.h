@@ -79,6 +79,9 @@ vxl_status launch_scene_noise(vxl_grid* g, uint32_t seed, float thresh, float fr
 vxl_status launch_scene_boxes(vxl_grid* g, uint32_t seed, int nboxes, int smin, int smax, cudaStream_t s);
 vxl_status launch_scene_terrain(vxl_grid* g, uint32_t seed, float base, float amp, float freq, int octaves,
                                 float* d_height, cudaStream_t s);
+vxl_status launch_light_points(vxl_ctx* ctx, const vxl_grid* g, const float* wpos, const float* nrm,
+                               const float* noise, int64_t npix, const vxl_light* lights, int nlights,
+                               unsigned long long* lit, unsigned long long* in_range, cudaStream_t s);
 vxl_status launch_volume_mips(vxl_ctx* ctx, const uint8_t* mip0, int sx, int sy, int sz, uint8_t* mip1, uint8_t* mip2,
                               cudaStream_t s);
 vxl_status launch_trace_primary(vxl_ctx* ctx, const vxl_volume* volumes, int nvol, const vxl_voxcmd* cmds, int ncmd,
