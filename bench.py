@@ -660,6 +660,31 @@ def run_gpu_frame(args):
         torch.mul(pos, 0.1, out=wpos)
         V.light_points(ctx, G, wpos, nrm, noise, npix, lights, lit, inr)
 
+    # temporal accumulation of a lighting buffer built from the occlusion terms
+    depth_t = torch.empty(npix, dtype=torch.float32, device="cuda")
+    light4 = torch.zeros(npix * 4, dtype=torch.float32, device="cuda")
+    last4 = torch.rand(npix * 4, dtype=torch.float32, device="cuda")
+    color3 = torch.full((npix * 3,), 0.5, dtype=torch.float32, device="cuda")
+    mat4 = torch.zeros(npix * 4, dtype=torch.float32, device="cuda")
+    motion2 = (torch.rand(npix * 2, dtype=torch.float32, device="cuda") - 0.5) * 2e-3
+    taa_out = torch.empty(npix * 4, dtype=torch.float32, device="cuda")
+
+    def taa_pass():
+        V.trace_primary(ctx, vs, worlds, vol_of, cam, tgt, W, H, pos, nrm, depth=depth_t)
+        occl()
+        lv = light4.view(npix, 4)
+        lv[:, 0] = outs["shadow"]
+        lv[:, 1] = outs["ao"]
+        lv[:, 2] = outs["spec"]
+        depth_t.div_(4096.0)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        V.light_taa(ctx, light4, last4, color3, nrm, mat4, depth_t, motion2, noise, W, H, taa_out)
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b)
+
     primary()
     torch.cuda.synchronize()
     valid = int((nrm.view(-1, 3).abs().sum(1) > 0).sum().item())
@@ -667,6 +692,7 @@ def run_gpu_frame(args):
         t_p = timed(primary)
         t_o = timed(occl)
         t_l = timed(lights_pass)
+        t_taa = statistics.median([taa_pass() for _ in range(max(3, args.steps // 4))]) / 1e3
         t_f = timed(lambda: (primary(), occl()))
     pairs = int(sum(bin(int(x)).count("1") for x in inr.cpu().numpy().view(np.uint64)))
     line = {
@@ -678,7 +704,7 @@ def run_gpu_frame(args):
                    "model_edges": [16, 64], "l2": "flushed between timed steps"},
         "primary_ms": t_p * 1e3, "primary_mpix_per_s": npix / t_p / 1e6, "occlusion_ms": t_o * 1e3,
         "occlusion_grays_per_s": valid * 10 / t_o / 1e9, "covered_pixels": valid,
-        "lights64_ms": t_l * 1e3, "light_rays": pairs, "light_grays_per_s": pairs / t_l / 1e9,
+        "taa_ms": t_taa * 1e3, "lights64_ms": t_l * 1e3, "light_rays": pairs, "light_grays_per_s": pairs / t_l / 1e9,
         "voxelize": {"seconds": t_vox, "instances": ninst}, "clocks": clk.summary(),
     }
     if not args.no_cpu_baseline:

@@ -260,6 +260,25 @@ vxl_status vxl_light_points(vxl_ctx* ctx, const vxl_grid* grid, const float* d_w
                             const float* d_noise, int64_t npix, const vxl_light* lights, int nlights,
                             uint64_t* d_lit, uint64_t* d_in_range, void* stream);
 
+/* Temporal accumulation of the lighting buffer (LightTAA.frag:37-141): the
+ * pass after the occlusion terms. Device fp32 images, [height][width][c]
+ * row-major, sampled with this library's sampler for the pass (bilinear,
+ * clamp to edge, texel centres at (i + 0.5) / size) at UV = ((px + .5) / W,
+ * (py + .5) / H); sin/cos are the library's own. Out: float[npix][4]
+ * (accumulated rgb, variance), the next frame's last_light. */
+typedef struct vxl_taa_frame {
+    const float* light;       /* [4] this frame's lighting */
+    const float* last_light;  /* [4] the previous output (rgb, variance in a) */
+    const float* color;       /* [3] albedo */
+    const float* normal;      /* [3] world normal */
+    const float* material;    /* [4] */
+    const float* depth;       /* [1] depth in [0, 1]; 1 = sky (copied through) */
+    const float* motion;      /* [2] UV offset to the previous frame */
+    const float* noise;       /* [4] blue-noise texel of getNoise() (x is used) */
+    int32_t width, height;
+} vxl_taa_frame;
+vxl_status vxl_light_taa(vxl_ctx* ctx, const vxl_taa_frame* frame, float* d_out, void* stream);
+
 /* ------------------------------------------------------------ voxelizer */
 typedef struct vxl_model {
     const uint8_t* data;   /* device palette indices [sz][sy][sx] (VoxAsset::PixelAt, VoxAsset.h:52-56) */

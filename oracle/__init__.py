@@ -146,6 +146,7 @@ def lib():
             L.vo_affine_inverse.argtypes = [fp, fp, fp]
             L.vo_primary.argtypes = [vp, vp, vp, ip, fp, ip, C.c_int, fp, fp, C.c_float, C.c_int, C.c_int, C.c_int,
                                      fp, fp, fp, ip, ip, C.c_int]
+            L.vo_taa.argtypes = [fp, fp, fp, fp, fp, fp, fp, fp, C.c_int, C.c_int, fp, C.c_int]
             L.vo_soft_render.argtypes = [fp, C.c_int, C.c_int, C.c_int, fp, fp, C.c_int, C.POINTER(SoftParams),
                                          vp, C.c_int64, C.c_double, vp, vp, C.c_int]
             _lib = L
@@ -498,6 +499,15 @@ def primary(volumes, worlds, vol_of, cam, target, W, H, frame=0, tan_half_fov=0.
                      _f(out["pos"]), _f(out["nrm"]), _f(out["depth"]), _i(out["material"]), _i(out["instance"]),
                      threads or threads_default())
     del keep
+    return out
+
+
+def taa(light, last, color, normal, material, depth, motion, noise, threads=None):
+    """LightTAA.frag main over [H, W, c] fp32 images; returns out [H, W, 4]."""
+    arrs = [np.ascontiguousarray(a, np.float32) for a in (light, last, color, normal, material, depth, motion, noise)]
+    H, W = arrs[0].shape[:2]
+    out = np.zeros((H, W, 4), np.float32)
+    lib().vo_taa(*[_f(a) for a in arrs], W, H, _f(out), threads or threads_default())
     return out
 
 

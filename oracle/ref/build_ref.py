@@ -24,6 +24,9 @@ output into oracle/_ref/ (git-ignored):
 * TransformSystem::RealculateMatrix (Sources/World/Systems/TransformSystem.cpp)
   is cut out, made a free function, and compiled in ref_transform_harness.cpp
   against the vendored glm.
+* main and luminance of Sources/Shaders/LightTAA.frag are cut out (main renamed
+  taa_main; assignments to a .xyz swizzle rewritten component-wise) and
+  compiled in ref_taa_harness.cpp with the library's bilinear sampler.
 
 Compiler flags: -O2 -ffp-contract=off -fsingle-precision-constant (GLSL float
 literals are single precision). Output: oracle/_ref/libvxl_ref.so.
@@ -56,7 +59,17 @@ def _glslpp(text: str) -> str:
     text = re.sub(r"\bout\s+vec3\s+", "vec3& ", text)
     text = re.sub(r"\bout\s+uint\s+", "uint& ", text)
     text = re.sub(r"\.([xyzw]{2,4})\b(?!\s*\()", r".\1()", text)
+    text = re.sub(r"\.([rgba]{2,4})\b(?!\s*\()", r".\1()", text)
     return text
+
+
+def _swizzle_assign(text: str) -> str:
+    """GLSL assignments to a .xyz swizzle (`v.xyz op= e;`) as component-wise C++."""
+    def rep(m):
+        v, op, e = m.group(1), m.group(2), m.group(3)
+        return ("{ vec3 _t(%s.x, %s.y, %s.z); _t %s (%s); %s.x = _t.x; %s.y = _t.y; %s.z = _t.z; }"
+                % (v, v, v, op, e, v, v, v))
+    return re.sub(r"\b(\w+)\.xyz\s*(\+=|-=|\*=|/=|=)\s*([^;]+);", rep, text)
 
 
 def _function(src: str, signature: str) -> str:
@@ -108,10 +121,14 @@ def generate() -> None:
     geo = open(os.path.join(sh, "GeometryVoxel.frag")).read()
     voxasset = open(os.path.join(r, "Sources", "Asset", "VoxAsset.cpp")).read()
     transform = open(os.path.join(r, "Sources", "World", "Systems", "TransformSystem.cpp")).read()
+    taa = open(os.path.join(sh, "LightTAA.frag")).read()
     parts = {
         "geometry_clip.inc": _glslpp(_function(geo, "vec3 clipToAABB(")),
         "geometry_intersect.inc": _glslpp(_function(geo, "bool intersectVolume(")),
         "voxasset_mip.inc": _braced_from(voxasset, "for (int x = 0; x < mipSizeX; x++)"),
+        "taa_main.inc": _glslpp(_swizzle_assign(_function(taa, "float luminance(") + "\n"
+                                                 + _function(taa, "void main()").replace("void main()",
+                                                                                         "void taa_main()", 1))),
         "transform_realculate.inc": _function(transform, "void TransformSystem::RealculateMatrix(").replace(
             "TransformSystem::", "", 1),
         "Light_frag.inc": _glslpp(light),
@@ -140,7 +157,8 @@ def build(force: bool = False, verbose: bool = False) -> str | None:
     if not available():
         return None
     srcs = [os.path.join(HERE, "ref_light_harness.cpp"), os.path.join(HERE, "ref_voxelizer_harness.cpp"),
-            os.path.join(HERE, "ref_geometry_harness.cpp"), os.path.join(HERE, "ref_transform_harness.cpp")]
+            os.path.join(HERE, "ref_geometry_harness.cpp"), os.path.join(HERE, "ref_transform_harness.cpp"),
+            os.path.join(HERE, "ref_taa_harness.cpp")]
     if not force and os.path.exists(SO) and os.path.getmtime(SO) >= max(os.path.getmtime(s) for s in srcs + [__file__]):
         return SO
     generate()
@@ -171,6 +189,10 @@ def build(force: bool = False, verbose: bool = False) -> str | None:
     o5 = os.path.join(OUT, "ref_transform.o")
     subprocess.run(common + ["-c", "-I", OUT, "-I", os.path.join(r, "Vendor"), srcs[3], "-o", o5], check=True)
     objs.append(o5)
+    # LightTAA.frag's main and luminance
+    o6 = os.path.join(OUT, "ref_taa.o")
+    subprocess.run(common + ["-c", "-I", OUT, "-I", os.path.join(r, "Vendor"), srcs[4], "-o", o6], check=True)
+    objs.append(o6)
     tmp = SO + ".tmp%d" % os.getpid()
     subprocess.run(["g++", "-shared", "-o", tmp] + objs, check=True)
     os.replace(tmp, SO)

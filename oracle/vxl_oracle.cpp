@@ -1373,3 +1373,174 @@ void vo_primary(const uint8_t* const* mip0s, const uint8_t* const* mip1s, const 
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Temporal accumulation: LightTAA.frag:37-141 (main), luminance :30-35.
+// Images are fp32 arrays, x fastest; texture() is this library's sampler:
+// bilinear, clamp to edge, texel centres at (i + 0.5) / size:
+//   x = u * W - 0.5, i0 = floor(x), a = x - i0 (same for y), taps clamped,
+//   v = (t00 (1-a) + t10 a)(1-b) + (t01 (1-a) + t11 a) b.
+// sin/cos are this library's own (sincos_own).
+namespace {
+
+struct Img {
+    const float* p;
+    int c;  // channels
+};
+struct TaaImgs {
+    Img light, last, color, normal, material, depth, motion;
+    int W, H;
+};
+
+void tex(const Img& im, int W, int H, float u, float v, float* out) {
+    const float x = u * (float)W - 0.5f, y = v * (float)H - 0.5f;
+    const float fx = std::floor(x), fy = std::floor(y);
+    const float ax = x - fx, ay = y - fy;
+    int x0 = (int)fx, y0 = (int)fy, x1 = x0 + 1, y1 = y0 + 1;
+    x0 = x0 < 0 ? 0 : (x0 > W - 1 ? W - 1 : x0);
+    x1 = x1 < 0 ? 0 : (x1 > W - 1 ? W - 1 : x1);
+    y0 = y0 < 0 ? 0 : (y0 > H - 1 ? H - 1 : y0);
+    y1 = y1 < 0 ? 0 : (y1 > H - 1 ? H - 1 : y1);
+    const float bx = 1.0f - ax, by = 1.0f - ay;
+    for (int k = 0; k < im.c; k++) {
+        const float t00 = im.p[((size_t)y0 * W + x0) * im.c + k], t10 = im.p[((size_t)y0 * W + x1) * im.c + k];
+        const float t01 = im.p[((size_t)y1 * W + x0) * im.c + k], t11 = im.p[((size_t)y1 * W + x1) * im.c + k];
+        const float top = t00 * bx + t10 * ax;
+        const float bot = t01 * bx + t11 * ax;
+        out[k] = top * by + bot * ay;
+    }
+    for (int k = im.c; k < 4; k++) out[k] = 0.0f;
+}
+inline float len2(float x, float y) { return std::sqrt(x * x + y * y); }
+inline float len3(const float* a, const float* b) {
+    const float dx = a[0] - b[0], dy = a[1] - b[1], dz = a[2] - b[2];
+    float d = dx * dx + dy * dy;
+    d = d + dz * dz;
+    return std::sqrt(d);
+}
+inline float len4(const float* a, const float* b) {
+    const float d0 = a[0] - b[0], d1 = a[1] - b[1], d2 = a[2] - b[2], d3 = a[3] - b[3];
+    float d = d0 * d0 + d1 * d1;
+    d = d + d2 * d2;
+    d = d + d3 * d3;
+    return std::sqrt(d);
+}
+inline float dot3(const float* a, const float* b) {
+    float d = a[0] * b[0] + a[1] * b[1];
+    return d + a[2] * b[2];
+}
+inline float clampf(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
+
+void taa_pixel(const TaaImgs& I, const float* noise, int px, int py, float* out) {
+    const int W = I.W, H = I.H;
+    const float FAR = 4096.0f;
+    const float GR = 2.118033988749895f;
+    const float iResx = 1.0f / (float)W, iResy = 1.0f / (float)H;
+    const float uvx = ((float)px + 0.5f) / (float)W, uvy = ((float)py + 0.5f) / (float)H;
+    float motion[4], cl[4], cc[4], cm[4], cn[4], cd[4], ll[4];
+    tex(I.motion, W, H, uvx, uvy, motion);
+    const float oux = uvx + motion[0], ouy = uvy + motion[1];
+    tex(I.light, W, H, uvx, uvy, cl);
+    tex(I.color, W, H, uvx, uvy, cc);
+    tex(I.material, W, H, uvx, uvy, cm);
+    tex(I.normal, W, H, uvx, uvy, cn);
+    tex(I.depth, W, H, uvx, uvy, cd);
+    const float depth = cd[0];
+    if (depth == 1.0f) {
+        for (int k = 0; k < 4; k++) out[k] = cl[k];
+        return;
+    }
+    tex(I.last, W, H, oux, ouy, ll);
+    float lastVariance = ll[3];
+    if (clampf(oux, 0.0f, 1.0f) != oux || clampf(ouy, 0.0f, 1.0f) != ouy) {
+        float count = 0.0f, s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+        for (int x = -9; x <= 9; ++x)
+            for (int y = -9; y <= 9; ++y) {
+                const float ox = (float)x * iResx, oy = (float)y * iResy;
+                const float u = clampf(uvx + ox, 0.001f, 0.999f), v = clampf(uvy + oy, 0.001f, 0.999f);
+                float nmo[4], nco[4], nno[4], nma[4], nde[4], nli[4];
+                tex(I.motion, W, H, u, v, nmo);
+                tex(I.color, W, H, u, v, nco);
+                tex(I.normal, W, H, u, v, nno);
+                tex(I.material, W, H, u, v, nma);
+                tex(I.depth, W, H, u, v, nde);
+                float factor = gmax(dot3(cn, nno), 0.0f);
+                factor *= glsl_step(0.8f, 1.0f - len4(cm, nma));
+                factor *= 1.0f - clampf(std::fabs(depth - nde[0]) * FAR, 0.0f, 1.0f);
+                factor *= 1.0f - clampf(len3(cc, nco), 0.0f, 1.0f);
+                if (len2(motion[0] - nmo[0], motion[1] - nmo[1]) > 0.1f) factor = 0.0f;
+                tex(I.light, W, H, u, v, nli);
+                s0 += factor * nli[0];
+                s1 += factor * nli[1];
+                s2 += factor * nli[2];
+                count += factor;
+            }
+        out[0] = s0 / count;
+        out[1] = s1 / count;
+        out[2] = s2 / count;
+        out[3] = 1.0f;
+        return;
+    }
+    float nmin[3] = {10000.0f, 10000.0f, 10000.0f}, nmax[3] = {0.0f, 0.0f, 0.0f};
+    float ncol[3] = {0.0f, 0.0f, 0.0f};
+    float diffSum = 1.0f, count = 0.0f;
+    const float size = 12.0f;
+    float radius = 1.0f;
+    const float dscale = gmin(gmax(0.1f, 0.5f), 1.0f / depth);  // clamp(0.1, 0.5, 1.0/currentDepth)
+    for (float angle = noise[0] * 3.1415f * GR; radius <= size; angle += 2.39f) {
+        radius += 1.0f;
+        float sn, cs;
+        sincos_own(angle, &sn, &cs);
+        const float rv = radius * (lastVariance + 1.0f);
+        const float ox = cs * iResx * rv * dscale, oy = sn * iResy * rv * dscale;
+        const float u = clampf(uvx + ox, 0.001f, 0.999f), v = clampf(uvy + oy, 0.001f, 0.999f);
+        float nmo[4], nco[4], nno[4], nma[4], nde[4], nli[4];
+        tex(I.motion, W, H, u, v, nmo);
+        tex(I.color, W, H, u, v, nco);
+        tex(I.normal, W, H, u, v, nno);
+        tex(I.material, W, H, u, v, nma);
+        tex(I.depth, W, H, u, v, nde);
+        float factor = 1.212f - radius / size;
+        factor *= glsl_step(0.8f, 1.0f - len4(cm, nma));
+        factor *= gmax(dot3(cn, nno), 0.0f);
+        factor *= 1.0f - clampf(std::fabs(depth - nde[0]) * FAR, 0.0f, 1.0f);
+        factor *= 1.0f - clampf(len3(cc, nco) * 10000.0f, 0.0f, 1.0f);
+        if (len2(motion[0] - nmo[0], motion[1] - nmo[1]) > 0.1f) factor = 0.0f;
+        tex(I.light, W, H, u, v, nli);
+        for (int k = 0; k < 3; k++) {
+            nmin[k] = gmin(nmin[k], nli[k]);
+            nmax[k] = gmax(nmax[k], nli[k]);
+            ncol[k] += factor * nli[k];
+        }
+        count += factor;
+        diffSum += len3(nli, cl) * factor;
+    }
+    for (int k = 0; k < 3; k++) {
+        cl[k] += ncol[k];
+        cl[k] /= count + 1.0f;
+    }
+    diffSum /= radius;
+    for (int k = 0; k < 3; k++) ll[k] = gmin(gmax(ll[k], nmin[k]), nmax[k]);
+    const float a0 = std::fabs(cl[0] - ll[0]), a1 = std::fabs(cl[1] - ll[1]), a2 = std::fabs(cl[2] - ll[2]);
+    float lum = a0 * 0.2125f + a1 * 0.7154f;
+    lum = lum + a2 * 0.0721f;
+    const float variance = clampf(lum * 5.5f, 0.0f, 1.0f);
+    lastVariance += variance;
+    lastVariance -= diffSum * 0.08f;
+    lastVariance += len2(motion[0], motion[1]) * 20.0f;
+    const float t = clampf(1.0f - lastVariance, 0.3f, 0.9f);
+    const float omt = 1.0f - t;
+    for (int k = 0; k < 3; k++) out[k] = cl[k] * omt + ll[k] * t;
+    out[3] = clampf(lastVariance * 0.7f, 0.0f, 1.0f);
+}
+
+}  // namespace
+
+extern "C" void vo_taa(const float* light, const float* last, const float* color, const float* normal,
+                       const float* material, const float* depth, const float* motion, const float* noise, int W,
+                       int H, float* out, int threads) {
+    TaaImgs I{{light, 4}, {last, 4}, {color, 3}, {normal, 3}, {material, 4}, {depth, 1}, {motion, 2}, W, H};
+    parallel_for(W * H, threads, [&](int i) {
+        taa_pixel(I, noise + 4 * (size_t)i, i % W, i / W, out + 4 * (size_t)i);
+    });
+}

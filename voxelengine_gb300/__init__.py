@@ -38,7 +38,7 @@ EXPORTED = [
     "vxl_grid_build_bricks", "vxl_grid_import_r8", "vxl_grid_export_r8", "vxl_grid_import_palette",
     "vxl_grid_count", "vxl_trace_rays", "vxl_trace_occlusion", "vxl_trace_occlusion_host", "vxl_batch_create",
     "vxl_batch_run", "vxl_batch_destroy", "vxl_batch_info", "vxl_light_ambient",
-    "vxl_light_reflection", "vxl_light_point", "vxl_light_points", "vxl_voxelize", "vxl_voxelize_noalloc", "vxl_shadowvox_update",
+    "vxl_light_reflection", "vxl_light_point", "vxl_light_points", "vxl_light_taa", "vxl_voxelize", "vxl_voxelize_noalloc", "vxl_shadowvox_update",
     "vxl_vox_destroyed",
     "vxl_trace_soft_fwd", "vxl_trace_soft_bwd", "vxl_volume_build_mips", "vxl_trace_primary",
     "vxl_asset_guid", "vxl_read_palette", "vxl_transform_matrix", "vxl_prefab_load", "vxl_prefab_info",
@@ -112,6 +112,12 @@ class PrimaryOut(C.Structure):
                 ("instance", C.c_void_p)]
 
 
+class TaaFrame(C.Structure):
+    _fields_ = [("light", C.c_void_p), ("last_light", C.c_void_p), ("color", C.c_void_p), ("normal", C.c_void_p),
+                ("material", C.c_void_p), ("depth", C.c_void_p), ("motion", C.c_void_p), ("noise", C.c_void_p),
+                ("width", C.c_int32), ("height", C.c_int32)]
+
+
 class Light(C.Structure):
     _fields_ = [("pos", C.c_float * 3), ("range", C.c_float), ("spot", C.c_int32), ("pad", C.c_int32 * 3)]
 
@@ -182,6 +188,7 @@ def lib():
         L.vxl_light_ambient.argtypes = [vp, vp, vp, vp, vp, vp, i64, vp, vp, vp, vp]
         L.vxl_light_reflection.argtypes = [vp, vp, vp, vp, vp, vp, vp, i64, vp, vp, vp]
         L.vxl_light_point.argtypes = [vp, vp, vp, vp, vp, i64, C.POINTER(f * 3), f, C.c_int, vp, vp, vp]
+        L.vxl_light_taa.argtypes = [vp, C.POINTER(TaaFrame), vp, vp]
         L.vxl_light_points.argtypes = [vp, vp, vp, vp, vp, i64, C.POINTER(Light), C.c_int, vp, vp, vp]
         L.vxl_voxelize.argtypes = [vp, vp, C.POINTER(Model), C.c_int, C.POINTER(Instance), C.c_int, vp, vp]
         L.vxl_voxelize_noalloc.argtypes = [C.POINTER(GridDesc), C.POINTER(Model), C.c_int, C.POINTER(Instance),
@@ -439,6 +446,12 @@ def light_point(ctx, grid, wpos, nrm, noise, npix, light_pos, light_range, spot,
     check(lib().vxl_light_point(ctx.handle, grid.handle, _ptr(wpos), _ptr(nrm), _ptr(noise), npix,
                                 C.byref(_f3(light_pos)), float(light_range), 1 if spot else 0, _ptr(shadow),
                                 _ptr(records), _stream(stream)))
+
+
+def light_taa(ctx, light, last_light, color, normal, material, depth, motion, noise, W, H, out, stream=None):
+    f = TaaFrame(_ptr(light), _ptr(last_light), _ptr(color), _ptr(normal), _ptr(material), _ptr(depth), _ptr(motion),
+                 _ptr(noise), W, H)
+    check(lib().vxl_light_taa(ctx.handle, C.byref(f), _ptr(out), _stream(stream)))
 
 
 def light_points(ctx, grid, wpos, nrm, noise, npix, lights, lit, in_range=None, stream=None):

@@ -572,6 +572,17 @@ vxl_status vxl_light_point(vxl_ctx* ctx, const vxl_grid* g, const float* d_wpos,
                               d_records, (cudaStream_t)stream);
 }
 
+vxl_status vxl_light_taa(vxl_ctx* ctx, const vxl_taa_frame* f, float* d_out, void* stream) {
+    if (!ctx || !f || !d_out) return fail(VXL_ERR_INVALID_ARG, "light_taa: NULL argument");
+    if (!f->light || !f->last_light || !f->color || !f->normal || !f->material || !f->depth || !f->motion ||
+        !f->noise)
+        return fail(VXL_ERR_INVALID_ARG, "light_taa: NULL image");
+    if (f->width < 1 || f->height < 1 || (int64_t)f->width * f->height > (int64_t)INT32_MAX / 4)
+        return fail(VXL_ERR_INVALID_ARG, "light_taa: bad image size");
+    VXL_TRY(set_device(ctx));
+    return launch_light_taa(ctx, f, d_out, (cudaStream_t)stream);
+}
+
 vxl_status vxl_light_points(vxl_ctx* ctx, const vxl_grid* g, const float* d_wpos, const float* d_nrm,
                             const float* d_noise, int64_t npix, const vxl_light* lights, int nlights,
                             uint64_t* d_lit, uint64_t* d_in_range, void* stream) {

@@ -79,6 +79,7 @@ vxl_status launch_scene_noise(vxl_grid* g, uint32_t seed, float thresh, float fr
 vxl_status launch_scene_boxes(vxl_grid* g, uint32_t seed, int nboxes, int smin, int smax, cudaStream_t s);
 vxl_status launch_scene_terrain(vxl_grid* g, uint32_t seed, float base, float amp, float freq, int octaves,
                                 float* d_height, cudaStream_t s);
+vxl_status launch_light_taa(vxl_ctx* ctx, const vxl_taa_frame* f, float* out, cudaStream_t s);
 vxl_status launch_light_points(vxl_ctx* ctx, const vxl_grid* g, const float* wpos, const float* nrm,
                                const float* noise, int64_t npix, const vxl_light* lights, int nlights,
                                unsigned long long* lit, unsigned long long* in_range, cudaStream_t s);
