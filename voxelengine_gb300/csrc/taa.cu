@@ -37,12 +37,45 @@ __device__ __forceinline__ void tex(const float* __restrict__ p, int W, int H, f
     y0 = y0 < 0 ? 0 : (y0 > H - 1 ? H - 1 : y0);
     y1 = y1 < 0 ? 0 : (y1 > H - 1 ? H - 1 : y1);
     const float bx = 1.0f - ax, by = 1.0f - ay;
+    const size_t i00 = ((size_t)y0 * W + x0) * C, i10 = ((size_t)y0 * W + x1) * C;
+    const size_t i01 = ((size_t)y1 * W + x0) * C, i11 = ((size_t)y1 * W + x1) * C;
+    float t00[C], t10[C], t01[C], t11[C];
+    if (C == 4) {  // 16-byte texels: one vector load each
+        const float4 a = __ldg(reinterpret_cast<const float4*>(p + i00)), b = __ldg(reinterpret_cast<const float4*>(p + i10));
+        const float4 c = __ldg(reinterpret_cast<const float4*>(p + i01)), d = __ldg(reinterpret_cast<const float4*>(p + i11));
+        const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+        const float cv[4] = {c.x, c.y, c.z, c.w}, dv[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+        for (int k = 0; k < C; k++) {
+            t00[k] = av[k];
+            t10[k] = bv[k];
+            t01[k] = cv[k];
+            t11[k] = dv[k];
+        }
+    } else if (C == 2) {
+        const float2 a = __ldg(reinterpret_cast<const float2*>(p + i00)), b = __ldg(reinterpret_cast<const float2*>(p + i10));
+        const float2 c = __ldg(reinterpret_cast<const float2*>(p + i01)), d = __ldg(reinterpret_cast<const float2*>(p + i11));
+        const float av[2] = {a.x, a.y}, bv[2] = {b.x, b.y}, cv[2] = {c.x, c.y}, dv[2] = {d.x, d.y};
+#pragma unroll
+        for (int k = 0; k < C; k++) {
+            t00[k] = av[k];
+            t10[k] = bv[k];
+            t01[k] = cv[k];
+            t11[k] = dv[k];
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < C; k++) {
+            t00[k] = __ldg(p + i00 + k);
+            t10[k] = __ldg(p + i10 + k);
+            t01[k] = __ldg(p + i01 + k);
+            t11[k] = __ldg(p + i11 + k);
+        }
+    }
 #pragma unroll
     for (int k = 0; k < C; k++) {
-        const float t00 = __ldg(p + ((size_t)y0 * W + x0) * C + k), t10 = __ldg(p + ((size_t)y0 * W + x1) * C + k);
-        const float t01 = __ldg(p + ((size_t)y1 * W + x0) * C + k), t11 = __ldg(p + ((size_t)y1 * W + x1) * C + k);
-        const float top = t00 * bx + t10 * ax;
-        const float bot = t01 * bx + t11 * ax;
+        const float top = t00[k] * bx + t10[k] * ax;
+        const float bot = t01[k] * bx + t11[k] * ax;
         out[k] = top * by + bot * ay;
     }
 }
@@ -65,11 +98,12 @@ __device__ __forceinline__ float dot3(const float* a, const float* b) {
     return d + a[2] * b[2];
 }
 
+// 32x4-pixel blocks: the spiral taps of neighbouring pixels overlap in L1
 __global__ void __launch_bounds__(128) k_taa(const TaaIn I, float* __restrict__ out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int W = I.W, H = I.H;
-    if (i >= W * H) return;
-    const int px = i % W, py = i / W;
+    const int px = blockIdx.x * 32 + (threadIdx.x & 31), py = blockIdx.y * 4 + (threadIdx.x >> 5);
+    if (px >= W || py >= H) return;
+    const int i = py * W + px;
     const float FAR = 4096.0f;
     const float GR = 2.118033988749895f;
     const float iResx = 1.0f / (float)W, iResy = 1.0f / (float)H;
@@ -188,8 +222,8 @@ __global__ void __launch_bounds__(128) k_taa(const TaaIn I, float* __restrict__ 
 vxl_status launch_light_taa(vxl_ctx* ctx, const vxl_taa_frame* f, float* out, cudaStream_t s) {
     TaaIn I{f->light, f->last_light, f->color, f->normal, f->material, f->depth, f->motion, f->noise, f->width,
             f->height};
-    const size_t n = (size_t)f->width * f->height;
-    k_taa<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(I, out);
+    const dim3 grid((unsigned)((f->width + 31) / 32), (unsigned)((f->height + 3) / 4));
+    k_taa<<<grid, 128, 0, s>>>(I, out);
     ctx->launches++;
     VXL_TRY_CUDA(cudaGetLastError());
     return VXL_OK;

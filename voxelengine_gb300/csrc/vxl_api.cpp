@@ -579,6 +579,9 @@ vxl_status vxl_light_taa(vxl_ctx* ctx, const vxl_taa_frame* f, float* d_out, voi
         return fail(VXL_ERR_INVALID_ARG, "light_taa: NULL image");
     if (f->width < 1 || f->height < 1 || (int64_t)f->width * f->height > (int64_t)INT32_MAX / 4)
         return fail(VXL_ERR_INVALID_ARG, "light_taa: bad image size");
+    if (((uintptr_t)f->light | (uintptr_t)f->last_light | (uintptr_t)f->material) & 15u ||
+        ((uintptr_t)f->motion & 7u))
+        return fail(VXL_ERR_INVALID_ARG, "light_taa: 4-channel images must be 16-byte and motion 8-byte aligned");
     VXL_TRY(set_device(ctx));
     return launch_light_taa(ctx, f, d_out, (cudaStream_t)stream);
 }
