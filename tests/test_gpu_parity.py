@@ -166,6 +166,27 @@ def test_occlusion_host_entry_matches_device(vxl, ctx):
         assert torch.equal(outs[k].cpu(), hout[k]), k
 
 
+@pytest.mark.parametrize("W,H", [(1280, 720), (1333, 777)])
+def test_occlusion_host_pipeline_matches_one_launch(vxl, ctx, W, H):
+    """Frames of >= 2^19 pixels go through the chunked copy/compute pipeline
+    (pixel chunks on two streams, global pixel index seeding the rays): the
+    outputs equal the one-launch device call bit for bit."""
+    import torch
+
+    G, cam, tgt, pos, nrm, rough = _c1_scene(vxl, ctx, 128, W, H)
+    npix = W * H
+    P = vxl.make_params(cam_pos=cam, n_ao=6, ao_len=24.0, n_spec=1, seed=5)
+    outs = {k: empty(npix, torch.float32) for k in ("shadow", "ao", "ao_vis", "spec", "spec_t")}
+    vxl.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, **outs)
+    hp, hn, hr = pos.cpu().pin_memory(), nrm.cpu().pin_memory(), rough.cpu().pin_memory()
+    hout = {k: torch.full((npix,), -3.0, dtype=torch.float32).pin_memory() for k in outs}
+    vxl.trace_occlusion_host(ctx, G, hp, hn, hr, npix, P, h_shadow=hout["shadow"], h_ao=hout["ao"],
+                             h_ao_vis=hout["ao_vis"], h_spec=hout["spec"], h_spec_t=hout["spec_t"])
+    torch.cuda.synchronize()
+    for k in outs:
+        assert torch.equal(outs[k].cpu(), hout[k]), k
+
+
 def test_light_passes_bit_exact(vxl, ctx, g64):
     import torch
 

@@ -46,7 +46,7 @@ struct SceneDesc {
     int64_t ntiles;
     int width, height;   // image size, for block tiles
     int tile_w;          // pixels per tile row; TP = runs of TP pixels
-    int pad;
+    uint32_t pix_base;   // added to the pixel index that seeds the ray generator (a chunk of a larger frame)
     TraceConstsP c;
 };
 
@@ -151,7 +151,7 @@ __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView&
         bool is_live = false;
         PSlot sl;
         if (kk < R && !sky) {
-            const f3 d = gen_dir(c, k, (uint32_t)gpix, P, N, T, B, ro);
+            const f3 d = gen_dir(c, k, (uint32_t)gpix + S.pix_base, P, N, T, B, ro);
             const float maxt = kind_maxt(c, k);
             int meta = (p << 4) | (k << 9);
             Hit h0{0, 0, 0, 0.0f, 0, VXL_RF_EXIT_BOUNDS};
@@ -397,7 +397,7 @@ static SceneDesc scene_of(const vxl_grid* g, const vxl_gbuffer* gb, const vxl_tr
     S.rec = o->records;
     S.npix = gb->npix;
     S.tile_begin = 0;
-    S.pad = 0;
+    S.pix_base = 0;
     const int TP = tune.tile_px;
     S.tile_w = TP;
     S.width = S.height = 0;
@@ -459,8 +459,10 @@ bool occl_pool_supported(const vxl_grid* g, const vxl_trace_params* p) {
 
 vxl_status launch_trace_occlusion_pool(vxl_ctx* ctx, const vxl_grid* g, const vxl_gbuffer* gb,
                                        const vxl_trace_params* p, const vxl_outputs* out,
-                                       unsigned long long* d_counter, const vxl_tuning& tune, cudaStream_t s) {
-    const SceneDesc S = scene_of(g, gb, p, out, tune);
+                                       unsigned long long* d_counter, const vxl_tuning& tune, cudaStream_t s,
+                                       uint32_t pix_base) {
+    SceneDesc S = scene_of(g, gb, p, out, tune);
+    S.pix_base = pix_base;
     VXL_TRY_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s));
     // per-ray records need the exact iteration count: no leaps there
     if (out->records) {

@@ -2,6 +2,7 @@
 // Validates arguments, owns contexts and grids, plans voxelizer runs, and
 // dispatches to the kernel launchers. Compiled without FMA contraction so the
 // host-side matrix arithmetic (glm::translate) matches the reference bit for bit.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -212,6 +213,10 @@ vxl_status vxl_ctx_destroy(vxl_ctx* ctx) {
     if (ctx->d_scratch) cudaFree(ctx->d_scratch);
     if (ctx->d_stage) cudaFree(ctx->d_stage);
     if (ctx->d_counters) cudaFree(ctx->d_counters);
+    if (ctx->pipe_ready) {
+        for (int k = 0; k < 2; k++) cudaStreamDestroy(ctx->pipe[k]);
+        cudaEventDestroy(ctx->pipe_start);
+    }
     delete ctx;
     return VXL_OK;
 }
@@ -417,17 +422,54 @@ vxl_status vxl_trace_occlusion_host(vxl_ctx* ctx, const vxl_grid* g, const float
     float* d_rough = (float*)(base + 2 * al(b3));
     float* outs[5];
     for (int k = 0; k < 5; k++) outs[k] = (float*)(base + 2 * al(b3) + (k + 1) * al(b1));
-    VXL_TRY_CUDA(cudaMemcpyAsync(d_pos, h_pos, b3, cudaMemcpyHostToDevice, s));
-    VXL_TRY_CUDA(cudaMemcpyAsync(d_nrm, h_nrm, b3, cudaMemcpyHostToDevice, s));
-    if (h_rough) VXL_TRY_CUDA(cudaMemcpyAsync(d_rough, h_rough, b1, cudaMemcpyHostToDevice, s));
-    vxl_gbuffer gb{d_pos, d_nrm, h_rough ? d_rough : nullptr, npix, 0, 0};
     float* hs[5] = {h_shadow, h_ao, h_ao_vis, h_spec, h_spec_t};
-    vxl_outputs o{hs[0] ? outs[0] : nullptr, hs[1] ? outs[1] : nullptr, hs[2] ? outs[2] : nullptr,
-                  hs[3] ? outs[3] : nullptr, hs[4] ? outs[4] : nullptr, nullptr};
-    VXL_TRY(launch_trace_occlusion(ctx, g, &gb, p, &o, s));
-    for (int k = 0; k < 5; k++)
-        if (hs[k]) VXL_TRY_CUDA(cudaMemcpyAsync(hs[k], outs[k], b1, cudaMemcpyDeviceToHost, s));
-    VXL_TRY_CUDA(cudaStreamSynchronize(s));
+    // Large frames run as a pipeline of pixel chunks on two streams, so the
+    // copies of one chunk overlap the tracing of its neighbours. A pixel's
+    // outputs depend only on its own rays, and the ray generator is seeded with
+    // the global pixel index (pix_base), so the result equals the one-launch form.
+    const int64_t kChunkMin = 1 << 18;
+    if (!occl_pool_supported(g, p) || npix < 2 * kChunkMin || npix > (int64_t)UINT32_MAX) {
+        VXL_TRY_CUDA(cudaMemcpyAsync(d_pos, h_pos, b3, cudaMemcpyHostToDevice, s));
+        VXL_TRY_CUDA(cudaMemcpyAsync(d_nrm, h_nrm, b3, cudaMemcpyHostToDevice, s));
+        if (h_rough) VXL_TRY_CUDA(cudaMemcpyAsync(d_rough, h_rough, b1, cudaMemcpyHostToDevice, s));
+        vxl_gbuffer gb{d_pos, d_nrm, h_rough ? d_rough : nullptr, npix, 0, 0};
+        vxl_outputs o{hs[0] ? outs[0] : nullptr, hs[1] ? outs[1] : nullptr, hs[2] ? outs[2] : nullptr,
+                      hs[3] ? outs[3] : nullptr, hs[4] ? outs[4] : nullptr, nullptr};
+        VXL_TRY(launch_trace_occlusion(ctx, g, &gb, p, &o, s));
+        for (int k = 0; k < 5; k++)
+            if (hs[k]) VXL_TRY_CUDA(cudaMemcpyAsync(hs[k], outs[k], b1, cudaMemcpyDeviceToHost, s));
+        VXL_TRY_CUDA(cudaStreamSynchronize(s));
+        return VXL_OK;
+    }
+    if (!ctx->pipe_ready) {
+        for (int k = 0; k < 2; k++) VXL_TRY_CUDA(cudaStreamCreateWithFlags(&ctx->pipe[k], cudaStreamNonBlocking));
+        VXL_TRY_CUDA(cudaEventCreateWithFlags(&ctx->pipe_start, cudaEventDisableTiming));
+        ctx->pipe_ready = true;
+    }
+    // the chunks start after the work already queued on the caller's stream
+    VXL_TRY_CUDA(cudaEventRecord(ctx->pipe_start, s));
+    for (int k = 0; k < 2; k++) VXL_TRY_CUDA(cudaStreamWaitEvent(ctx->pipe[k], ctx->pipe_start, 0));
+    const int64_t nchunks = std::min<int64_t>(8, npix / kChunkMin);
+    int64_t chunk = (npix + nchunks - 1) / nchunks;
+    chunk = (chunk + 1023) & ~(int64_t)1023;
+    int c = 0;
+    for (int64_t p0 = 0; p0 < npix; p0 += chunk, c++) {
+        const int64_t n = std::min(chunk, npix - p0);
+        cudaStream_t cs = ctx->pipe[c & 1];
+        VXL_TRY_CUDA(cudaMemcpyAsync(d_pos + 3 * p0, h_pos + 3 * p0, (size_t)n * 12, cudaMemcpyHostToDevice, cs));
+        VXL_TRY_CUDA(cudaMemcpyAsync(d_nrm + 3 * p0, h_nrm + 3 * p0, (size_t)n * 12, cudaMemcpyHostToDevice, cs));
+        if (h_rough)
+            VXL_TRY_CUDA(cudaMemcpyAsync(d_rough + p0, h_rough + p0, (size_t)n * 4, cudaMemcpyHostToDevice, cs));
+        vxl_gbuffer gb{d_pos + 3 * p0, d_nrm + 3 * p0, h_rough ? d_rough + p0 : nullptr, n, 0, 0};
+        vxl_outputs o{hs[0] ? outs[0] + p0 : nullptr, hs[1] ? outs[1] + p0 : nullptr, hs[2] ? outs[2] + p0 : nullptr,
+                      hs[3] ? outs[3] + p0 : nullptr, hs[4] ? outs[4] + p0 : nullptr, nullptr};
+        VXL_TRY(launch_trace_occlusion_pool(ctx, g, &gb, p, &o, ctx_next_counter(ctx), ctx->tune, cs,
+                                            (uint32_t)p0));
+        for (int k = 0; k < 5; k++)
+            if (hs[k])
+                VXL_TRY_CUDA(cudaMemcpyAsync(hs[k] + p0, outs[k] + p0, (size_t)n * 4, cudaMemcpyDeviceToHost, cs));
+    }
+    for (int k = 0; k < 2; k++) VXL_TRY_CUDA(cudaStreamSynchronize(ctx->pipe[k]));
     return VXL_OK;
 }
 

@@ -23,6 +23,10 @@ struct vxl_ctx {
     unsigned long long* d_counters;
     uint32_t counter_next;
     vxl_tuning tune;  // occlusion kernel launch shape (vxl_ctx_set_tuning)
+    // copy / compute pipeline of the host-buffer entry point (created on first use)
+    cudaStream_t pipe[2];
+    cudaEvent_t pipe_start;
+    bool pipe_ready;
 };
 constexpr uint32_t kCounterRing = 4096;
 
@@ -104,7 +108,8 @@ vxl_status launch_trace_occlusion(vxl_ctx* ctx, const vxl_grid* g, const vxl_gbu
 bool occl_pool_supported(const vxl_grid* g, const vxl_trace_params* p);
 vxl_status launch_trace_occlusion_pool(vxl_ctx* ctx, const vxl_grid* g, const vxl_gbuffer* gb,
                                        const vxl_trace_params* p, const vxl_outputs* out,
-                                       unsigned long long* d_counter, const vxl_tuning& tune, cudaStream_t s);
+                                       unsigned long long* d_counter, const vxl_tuning& tune, cudaStream_t s,
+                                       uint32_t pix_base = 0);
 unsigned long long* ctx_next_counter(vxl_ctx* ctx);
 // batched occlusion: scene table built on the host, uploaded once, one launch
 size_t batch_desc_bytes();
