@@ -447,8 +447,9 @@ typedef struct vxl_primary_out {
  * clipToAABB + intersectVolume (GeometryVoxel.frag:50-125, LOD and
  * transparency on, UV = ((px + .5) * 2 / W - 1, (py + .5) * 2 / H - 1)); the
  * nearest hit by view depth wins, ties to the lower command index. Host
- * arrays; returns after one read-back (the screen-bin size) with the frame
- * queued on `stream`. */
+ * arrays, copied before the call returns; the frame is queued on `stream`
+ * without waiting for it. Screen-bin lists are sized from the previous
+ * frame's; a frame that outgrows them scans every command (same result). */
 vxl_status vxl_trace_primary(vxl_ctx* ctx, const vxl_volume* volumes, int nvolumes, const vxl_voxcmd* cmds, int ncmds,
                              const vxl_camera* camera, const vxl_primary_out* out, void* stream);
 

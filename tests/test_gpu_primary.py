@@ -166,3 +166,33 @@ def test_frame_path_primary_then_occlusion(vxl, ctx):
         assert same_bits(outs[k].cpu().numpy(), wo[k]).all(), k
     hit = want["instance"] >= 0
     assert hit.mean() > 0.2 and (wo["shadow"][hit] == 0).any() and (wo["shadow"][hit] == 1).any()
+
+
+def test_primary_list_overflow_is_exact(vxl, ctx):
+    """A frame whose screen-bin lists outgrow the capacity sized from the
+    previous frame scans every command instead (same result); the next frame
+    runs with grown lists."""
+    rng = np.random.default_rng(41)
+    vols = _volumes(9, 3, 32, 40)
+    c2 = vxl.Context(0)  # fresh list capacity
+    W, H = 128, 96
+    cam = np.array([2.0, 2.0, -6.0], np.float32)
+    tgt = np.array([2.0, 2.0, 2.0], np.float32)
+    few_w, few_v = _instances(rng, 1, vols, 32)
+    _run_primary(vxl, c2, vols, few_w, few_v, cam, tgt, W, H, 0)
+    # 600 boxes of 3.2-4 world units 2.5-4.5 units in front of the camera: each
+    # covers most of the 8x6 screen tiles, far beyond the 16 per command the
+    # capacity allows for
+    many = []
+    for _ in range(600):
+        m = np.eye(4, dtype=np.float32)
+        m[:3, 3] = rng.uniform(-0.5, 2.5, 3)
+        m[2, 3] = rng.uniform(-3.5, -1.5)
+        many.append(np.ascontiguousarray(m.T).reshape(16))
+    many = np.array(many, np.float32)
+    many_v = rng.integers(0, len(vols), len(many)).astype(np.int32)
+    want = oracle.primary(vols, many, many_v, cam, tgt, W, H, frame=0)
+    for _ in range(2):  # first call overflows, second runs with grown lists
+        got = _run_primary(vxl, c2, vols, many, many_v, cam, tgt, W, H, 0)
+        _assert_same(got, want)
+    assert (want["instance"] >= 0).mean() > 0.5

@@ -17,6 +17,8 @@
 // `hitPos*0.1` and `*10.0`); output positions are in fine-voxel units
 // (world * 10), the ShadowVox grid's units, so the G-buffer feeds
 // vxl_trace_occlusion directly.
+#include <algorithm>
+#include <cstring>
 #include <vector>
 
 #include "vxl_device.cuh"
@@ -221,8 +223,10 @@ __global__ void k_prim_scan(const int* __restrict__ counts, int ntiles, int* __r
     if (threadIdx.x == 0) offsets[ntiles] = carry;
 }
 
+// entries beyond the list capacity are dropped; k_primary then scans every
+// instance for every tile (exact, slower) and the host grows the lists
 __global__ void k_prim_fill(const PrimInst* __restrict__ insts, int n, int tiles_x, const int* __restrict__ offsets,
-                            int* __restrict__ cursor, int* __restrict__ lists) {
+                            int* __restrict__ cursor, int* __restrict__ lists, int64_t cap) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const PrimInst& P = insts[k];
@@ -230,7 +234,8 @@ __global__ void k_prim_fill(const PrimInst* __restrict__ insts, int n, int tiles
     for (int ty = P.ty0; ty <= P.ty1; ty++)
         for (int tx = P.tx0; tx <= P.tx1; tx++) {
             const int t = ty * tiles_x + tx;
-            lists[offsets[t] + atomicAdd(&cursor[t], 1)] = k;
+            const int64_t at = (int64_t)offsets[t] + atomicAdd(&cursor[t], 1);
+            if (at < cap) lists[at] = k;
         }
 }
 
@@ -320,11 +325,12 @@ __device__ __forceinline__ bool intersect_volume(const VolDev& V, f3 origin, f3 
 // instances' nearest corner depth; a pixel stops scanning a chunk once that
 // depth, less a safety margin for rounding, is beyond its current hit (no
 // instance further in the chunk can be nearer).
-__global__ void __launch_bounds__(256) k_primary(const PrimInst* __restrict__ insts, const VolDev* __restrict__ vols,
-                                                 PrimCam C, const int* __restrict__ offsets,
-                                                 const int* __restrict__ lists, float* __restrict__ pos,
-                                                 float* __restrict__ nrm, float* __restrict__ depth,
-                                                 int32_t* __restrict__ material, int32_t* __restrict__ instance) {
+__global__ void __launch_bounds__(256, 3) k_primary(const PrimInst* __restrict__ insts, const VolDev* __restrict__ vols,
+                                                    PrimCam C, const int* __restrict__ offsets,
+                                                    const int* __restrict__ lists, int64_t cap, int ninst,
+                                                    float* __restrict__ pos, float* __restrict__ nrm,
+                                                    float* __restrict__ depth, int32_t* __restrict__ material,
+                                                    int32_t* __restrict__ instance) {
     __shared__ float s_near[256];
     __shared__ int s_id[256];
     const int tile = blockIdx.x;
@@ -341,12 +347,14 @@ __global__ void __launch_bounds__(256) k_primary(const PrimInst* __restrict__ in
     int bi = -1;
     f3 bp = mk(0.0f, 0.0f, 0.0f), bn = mk(0.0f, 0.0f, 0.0f);
     uint32_t bm = 0;
-    const int e0 = offsets[tile], e1 = offsets[tile + 1];
+    // lists that overflowed their capacity: every instance, in index order
+    const bool all = (int64_t)offsets[C.tiles_x * C.tiles_y] > cap;
+    const int e0 = all ? 0 : offsets[tile], e1 = all ? ninst : offsets[tile + 1];
     for (int c0 = e0; c0 < e1; c0 += 256) {
         const int cn = min(256, e1 - c0);
         __syncthreads();
         if ((int)threadIdx.x < cn) {
-            const int k = lists[c0 + threadIdx.x];
+            const int k = all ? c0 + (int)threadIdx.x : lists[c0 + threadIdx.x];
             s_id[threadIdx.x] = k;
             s_near[threadIdx.x] = insts[k].near;
         } else {
@@ -517,8 +525,37 @@ vxl_status launch_trace_primary(vxl_ctx* ctx, const vxl_volume* volumes, int nvo
             hv[v].dz[q] = mip_dim(hv[v].dz[q - 1]);
         }
     }
-    VXL_TRY_CUDA(cudaMemcpyAsync(d_vol, hv.data(), sizeof(VolDev) * (size_t)nvol, cudaMemcpyHostToDevice, s));
-    if (n > 0) VXL_TRY_CUDA(cudaMemcpyAsync(d_cmd, cmds, sizeof(vxl_voxcmd) * (size_t)n, cudaMemcpyHostToDevice, s));
+    // the previous frame's staging copy and list-size read-back have finished
+    // (normally long ago) before the pinned buffers are reused
+    if (ctx->pev) VXL_TRY_CUDA(cudaEventSynchronize(ctx->pev));
+    const size_t b_vol_h = sizeof(VolDev) * (size_t)nvol, b_cmd_h = sizeof(vxl_voxcmd) * (size_t)n;
+    if (ctx->h_pin_bytes < b_vol_h + b_cmd_h) {
+        if (ctx->h_pin) cudaFreeHost(ctx->h_pin);
+        ctx->h_pin = nullptr;
+        ctx->h_pin_bytes = 0;
+        const size_t want = (b_vol_h + b_cmd_h) * 3 / 2 + 4096;
+        VXL_TRY_CUDA(cudaHostAlloc(&ctx->h_pin, want, cudaHostAllocDefault));
+        ctx->h_pin_bytes = want;
+    }
+    if (!ctx->h_ptotal) {
+        VXL_TRY_CUDA(cudaHostAlloc((void**)&ctx->h_ptotal, sizeof(int), cudaHostAllocDefault));
+        *ctx->h_ptotal = 0;
+    }
+    if (!ctx->pev) VXL_TRY_CUDA(cudaEventCreateWithFlags(&ctx->pev, cudaEventDisableTiming));
+    // list capacity from the previous frame's total (and a floor for the first)
+    const int64_t want_cap = std::max<int64_t>((int64_t)*ctx->h_ptotal, (int64_t)n * 16 + ntiles);
+    if ((int64_t)ctx->plist_cap < want_cap) {
+        if (ctx->d_plist) VXL_TRY_CUDA(cudaFree(ctx->d_plist));
+        ctx->d_plist = nullptr;
+        ctx->plist_cap = 0;
+        const size_t cap = (size_t)want_cap * 3 / 2;
+        VXL_TRY_CUDA(cudaMalloc((void**)&ctx->d_plist, cap * sizeof(int)));
+        ctx->plist_cap = cap;
+    }
+    std::memcpy(ctx->h_pin, hv.data(), b_vol_h);
+    if (n > 0) std::memcpy((char*)ctx->h_pin + b_vol_h, cmds, b_cmd_h);
+    VXL_TRY_CUDA(cudaMemcpyAsync(d_vol, ctx->h_pin, b_vol_h, cudaMemcpyHostToDevice, s));
+    if (n > 0) VXL_TRY_CUDA(cudaMemcpyAsync(d_cmd, (char*)ctx->h_pin + b_vol_h, b_cmd_h, cudaMemcpyHostToDevice, s));
     VXL_TRY_CUDA(cudaMemsetAsync(d_count, 0, sizeof(int) * (size_t)(ntiles + 1), s));
     VXL_TRY_CUDA(cudaMemsetAsync(d_cur, 0, sizeof(int) * (size_t)(ntiles + 1), s));
     if (n > 0) {
@@ -528,20 +565,16 @@ vxl_status launch_trace_primary(vxl_ctx* ctx, const vxl_volume* volumes, int nvo
     k_prim_scan<<<1, 1024, 0, s>>>(d_count, ntiles, d_off);
     ctx->launches++;
     VXL_TRY_CUDA(cudaGetLastError());
-    // list length: one read-back per frame sizes the instance lists
-    int total = 0;
-    VXL_TRY_CUDA(cudaMemcpyAsync(&total, d_off + ntiles, sizeof(int), cudaMemcpyDeviceToHost, s));
-    VXL_TRY_CUDA(cudaStreamSynchronize(s));
-    if (total < 0) return fail(VXL_ERR_OUT_OF_RANGE, "trace_primary: instance lists exceed 2^31 entries");
-    void* lp;
-    VXL_TRY(ctx_stage(ctx, sizeof(int) * (size_t)(total > 0 ? total : 1), &lp));
-    int* d_lists = (int*)lp;
-    if (n > 0 && total > 0) {
-        k_prim_fill<<<blocks_of((size_t)n, 128), 128, 0, s>>>(d_ins, n, C.tiles_x, d_off, d_cur, d_lists);
+    // the list length goes back to the host without a wait; it sizes the next frame's lists
+    VXL_TRY_CUDA(cudaMemcpyAsync(ctx->h_ptotal, d_off + ntiles, sizeof(int), cudaMemcpyDeviceToHost, s));
+    VXL_TRY_CUDA(cudaEventRecord(ctx->pev, s));
+    const int64_t cap = (int64_t)ctx->plist_cap;
+    if (n > 0) {
+        k_prim_fill<<<blocks_of((size_t)n, 128), 128, 0, s>>>(d_ins, n, C.tiles_x, d_off, d_cur, ctx->d_plist, cap);
         ctx->launches++;
     }
-    k_primary<<<ntiles, kPrimTile * kPrimTile, 0, s>>>(d_ins, d_vol, C, d_off, d_lists, out->pos, out->nrm, out->depth,
-                                                       out->material, out->instance);
+    k_primary<<<ntiles, kPrimTile * kPrimTile, 0, s>>>(d_ins, d_vol, C, d_off, ctx->d_plist, cap, n, out->pos,
+                                                       out->nrm, out->depth, out->material, out->instance);
     ctx->launches++;
     VXL_TRY_CUDA(cudaGetLastError());
     return VXL_OK;

@@ -217,6 +217,13 @@ vxl_status vxl_ctx_destroy(vxl_ctx* ctx) {
         for (int k = 0; k < 2; k++) cudaStreamDestroy(ctx->pipe[k]);
         cudaEventDestroy(ctx->pipe_start);
     }
+    if (ctx->pev) {
+        cudaEventSynchronize(ctx->pev);
+        cudaEventDestroy(ctx->pev);
+    }
+    if (ctx->d_plist) cudaFree(ctx->d_plist);
+    if (ctx->h_ptotal) cudaFreeHost(ctx->h_ptotal);
+    if (ctx->h_pin) cudaFreeHost(ctx->h_pin);
     delete ctx;
     return VXL_OK;
 }

@@ -27,6 +27,15 @@ struct vxl_ctx {
     cudaStream_t pipe[2];
     cudaEvent_t pipe_start;
     bool pipe_ready;
+    // primary visibility: screen-tile instance lists (grown from the previous
+    // frame's size, read back asynchronously), pinned staging for the
+    // command table, and the event after that frame's staging copy / read-back
+    int* d_plist;
+    size_t plist_cap;
+    int* h_ptotal;
+    void* h_pin;
+    size_t h_pin_bytes;
+    cudaEvent_t pev;
 };
 constexpr uint32_t kCounterRing = 4096;
 
