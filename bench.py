@@ -626,8 +626,10 @@ def run_gpu_frame(args):
                                                                                 "spec_t")}
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
 
+    cmd_table = V.voxcmds(worlds, vol_of)  # the engine's per-frame command buffer (GeometryVoxelPipeline::Cmd)
+
     def primary():
-        V.trace_primary(ctx, vs, worlds, vol_of, cam, tgt, W, H, pos, nrm)
+        V.trace_primary(ctx, vs, None, None, cam, tgt, W, H, pos, nrm, cmds=cmd_table)
 
     def occl():
         V.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, width=W, height=H, **outs)
@@ -670,7 +672,7 @@ def run_gpu_frame(args):
     taa_out = torch.empty(npix * 4, dtype=torch.float32, device="cuda")
 
     def taa_pass():
-        V.trace_primary(ctx, vs, worlds, vol_of, cam, tgt, W, H, pos, nrm, depth=depth_t)
+        V.trace_primary(ctx, vs, None, None, cam, tgt, W, H, pos, nrm, depth=depth_t, cmds=cmd_table)
         occl()
         lv = light4.view(npix, 4)
         lv[:, 0] = outs["shadow"]

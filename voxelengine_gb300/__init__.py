@@ -540,15 +540,28 @@ class VolumeSet:
         return len(self.mips)
 
 
-def trace_primary(ctx, volset: VolumeSet, worlds, vol_of, cam, target, W, H, pos, nrm, depth=None, material=None,
-                  instance=None, frame=0, tan_half_fov=0.57735026, stream=None):
-    """vxl_trace_primary; worlds float[n, 16] column-major, vol_of int[n]; camera in world units."""
+VOXCMD_DTYPE = np.dtype([("world", "<f4", (16,)), ("volume", "<i4"), ("palette", "<i4")])
+
+
+def voxcmds(worlds, vol_of, palette=None) -> np.ndarray:
+    """The command table of vxl_trace_primary as a numpy record array (layout of vxl_voxcmd)."""
     worlds = np.ascontiguousarray(worlds, np.float32).reshape(-1, 16)
-    n = worlds.shape[0]
-    rec = np.zeros(max(1, n), dtype=[("world", "<f4", (16,)), ("volume", "<i4"), ("palette", "<i4")])
-    if n:
-        rec["world"] = worlds
-        rec["volume"] = np.asarray(vol_of, np.int32)
+    rec = np.zeros(worlds.shape[0], dtype=VOXCMD_DTYPE)
+    rec["world"] = worlds
+    rec["volume"] = np.asarray(vol_of, np.int32)
+    if palette is not None:
+        rec["palette"] = np.asarray(palette, np.int32)
+    return rec
+
+
+def trace_primary(ctx, volset: VolumeSet, worlds, vol_of, cam, target, W, H, pos, nrm, depth=None, material=None,
+                  instance=None, frame=0, tan_half_fov=0.57735026, stream=None, cmds=None):
+    """vxl_trace_primary; worlds float[n, 16] column-major, vol_of int[n] (or a prebuilt
+    `cmds` table from voxcmds()); camera in world units."""
+    rec = cmds if cmds is not None else voxcmds(worlds, vol_of)
+    n = rec.shape[0]
+    if n == 0:
+        rec = np.zeros(1, dtype=VOXCMD_DTYPE)
     cmds = rec.ctypes.data_as(C.POINTER(VoxCmd))
     c = Camera()
     c.pos[:] = [float(x) for x in cam]
