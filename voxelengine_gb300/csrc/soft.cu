@@ -230,8 +230,7 @@ __global__ void __launch_bounds__(1024) k_soft_bwd(const SoftConsts c, const flo
     const float w0 = g0 * rs.y * kk, w1 = g1 * rs.z * kk, w2 = g2 * rs.w * kk;
     const float wsum = (w0 + w1) + w2;
 
-    int cidx[kSoftMaxCells];
-    float cpre[kSoftMaxCells];
+    int2 cell[kSoftMaxCells];  // (voxel index, prefix transmittance bits): one 8-byte local store per cell
     int m = 0;
     {
         CellWalk w;
@@ -241,8 +240,7 @@ __global__ void __launch_bounds__(1024) k_soft_bwd(const SoftConsts c, const flo
             if (w.cx < c.nx && w.cy < c.ny && w.cz < c.nz) {
                 const int idx = w.cx + w.cy * c.nx + w.cz * c.nx * c.ny;
                 const float a = soft_clamp(__ldg(&c.vox[idx].x));
-                cidx[m] = idx;
-                cpre[m] = T;
+                cell[m] = make_int2(idx, __float_as_int(T));
                 m++;
                 T = T * (1.0f - a);
                 if (T < kSoftTmin) break;
@@ -253,8 +251,9 @@ __global__ void __launch_bounds__(1024) k_soft_bwd(const SoftConsts c, const flo
     // suffix pass: suf = prod_{l>j} (1 - a_l); S = colour seen from just past j
     float suf = 1.0f, S0 = 0.0f, S1 = 0.0f, S2 = 0.0f;
     for (int j = m - 1; j >= 0; j--) {
-        const int idx = cidx[j];
-        const float pre = cpre[j];
+        const int2 ce = cell[j];
+        const int idx = ce.x;
+        const float pre = __int_as_float(ce.y);
         const float4 v = __ldg(c.vox + idx);
         const float a = soft_clamp(v.x);
         const float dcl = (v.x >= 0.0f && v.x <= kSoftAmax) ? 1.0f : 0.0f;
