@@ -4,7 +4,7 @@ band pushed off screen (the disocclusion branch), sky pixels (depth 1)."""
 import numpy as np
 
 
-def frame(W, H, seed):
+def frame(W, H, seed, band=4):
     rng = np.random.default_rng(seed)
     yy, xx = np.mgrid[0:H, 0:W].astype(np.float32)
     region = ((xx // 11 + yy // 7) % 3).astype(np.int32)
@@ -19,7 +19,7 @@ def frame(W, H, seed):
     depth = (0.05 + 0.02 * region + 1e-4 * xx).astype(np.float32)
     depth[(yy < 3)] = 1.0  # sky rows
     motion = (rng.normal(size=(H, W, 2)) * 2e-3).astype(np.float32)
-    motion[:, :4, 0] = -0.2  # pushed off the left edge: disocclusion branch
+    motion[:, :band, 0] = -0.2  # pushed off the left edge: disocclusion branch
     noise = rng.random((H, W, 4)).astype(np.float32)
     f = lambda a: np.ascontiguousarray(a, np.float32)
     return dict(light=f(light), last=f(last), color=f(color), normal=f(normal), material=f(material),

@@ -33,7 +33,7 @@ vxl_status cuda_fail(cudaError_t e, const char* what) {
                 cudaGetErrorString(e), cudaGetErrorName(e));
 }
 
-static vxl_status grow(void** p, size_t* have, size_t need) {
+vxl_status ctx_grow(void** p, size_t* have, size_t need) {
     if (*have >= need) return VXL_OK;
     size_t n = *have ? *have : (size_t)1 << 20;
     while (n < need) n *= 2;
@@ -47,12 +47,12 @@ static vxl_status grow(void** p, size_t* have, size_t need) {
 }
 
 vxl_status ctx_scratch(vxl_ctx* ctx, size_t bytes, void** out) {
-    VXL_TRY(grow(&ctx->d_scratch, &ctx->d_scratch_bytes, bytes));
+    VXL_TRY(ctx_grow(&ctx->d_scratch, &ctx->d_scratch_bytes, bytes));
     *out = ctx->d_scratch;
     return VXL_OK;
 }
 vxl_status ctx_stage(vxl_ctx* ctx, size_t bytes, void** out) {
-    VXL_TRY(grow(&ctx->d_stage, &ctx->d_stage_bytes, bytes));
+    VXL_TRY(ctx_grow(&ctx->d_stage, &ctx->d_stage_bytes, bytes));
     *out = ctx->d_stage;
     return VXL_OK;
 }
@@ -224,6 +224,7 @@ vxl_status vxl_ctx_destroy(vxl_ctx* ctx) {
     if (ctx->d_plist) cudaFree(ctx->d_plist);
     if (ctx->h_ptotal) cudaFreeHost(ctx->h_ptotal);
     if (ctx->h_pin) cudaFreeHost(ctx->h_pin);
+    if (ctx->d_taa) cudaFree(ctx->d_taa);
     delete ctx;
     return VXL_OK;
 }

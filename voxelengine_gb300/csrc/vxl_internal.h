@@ -36,6 +36,9 @@ struct vxl_ctx {
     void* h_pin;
     size_t h_pin_bytes;
     cudaEvent_t pev;
+    // temporal accumulation: the per-texel records the spiral taps read
+    void* d_taa;
+    size_t taa_bytes;
 };
 constexpr uint32_t kCounterRing = 4096;
 
@@ -68,6 +71,8 @@ vxl_status cuda_fail(cudaError_t e, const char* what);
 
 // device scratch owned by the context (grows, never shrinks)
 vxl_status ctx_scratch(vxl_ctx* ctx, size_t bytes, void** out);
+// grows a context-owned device buffer to at least `need` bytes (contents not kept)
+vxl_status ctx_grow(void** p, size_t* have, size_t need);
 vxl_status ctx_stage(vxl_ctx* ctx, size_t bytes, void** out);
 
 struct DevInstance {
