@@ -121,6 +121,11 @@ def test_primary_edge_cases(vxl, ctx):
         vxl.trace_primary(ctx, vs, np.eye(4, dtype=np.float32).reshape(1, 16), [5], (0, 1, -5), (0, 0, 0), W, H,
                           pos, nrm)
     assert e.value.status == vxl.VXL_ERR_OUT_OF_RANGE
+    # more (command, screen tile) pairs than 32-bit list offsets hold are rejected before any work
+    many = np.tile(np.eye(4, dtype=np.float32).reshape(1, 16), (2100, 1))
+    with pytest.raises(vxl.VxlError) as e:
+        vxl.trace_primary(ctx, vs, many, [0] * 2100, (0, 1, -5), (0, 0, 0), 16384, 16384, pos, nrm)
+    assert e.value.status == vxl.VXL_ERR_INVALID_ARG
     # volumes smaller than 4 on an axis are rejected (VoxAsset sizes are multiples of 4)
     d0 = torch.zeros(2 * 8 * 8, dtype=torch.uint8, device="cuda")
     with pytest.raises(vxl.VxlError):

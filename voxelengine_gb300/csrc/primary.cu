@@ -120,10 +120,47 @@ __device__ __forceinline__ void affine_inverse(const float* m, float* ri, float*
 // Per instance: inverse, local camera, and the screen tiles its volume box
 // can cover (the 8 corners projected with a margin; the full screen when a
 // corner is not in front of the camera). Writes the tile count of each.
+// The tiles of the 32 rectangles a warp's lanes hold, spread over its lanes:
+// rectangle j of lane j is visited by all lanes (tile q of its row-major order
+// by lane q mod 32), so one instance covering much of the screen does not
+// leave its tiles to one thread. Called by whole warps (empty rectangles for
+// lanes past the end); f(j, tile) runs once per tile of rectangle j.
+template <class F>
+__device__ __forceinline__ void warp_rects(int tx0, int ty0, int tx1, int ty1, int tiles_x, F f) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    for (int j = 0; j < 32; j++) {
+        const int a0 = __shfl_sync(full, tx0, j), b0 = __shfl_sync(full, ty0, j);
+        const int a1 = __shfl_sync(full, tx1, j), b1 = __shfl_sync(full, ty1, j);
+        const int w = a1 - a0 + 1, h = b1 - b0 + 1;
+        if (w <= 0 || h <= 0) continue;
+        const int cnt = w * h;
+        for (int q = lane; q < cnt; q += 32) f(j, (b0 + q / w) * tiles_x + a0 + q % w);
+    }
+}
+
+__device__ __forceinline__ void prim_prep_one(const vxl_voxcmd* __restrict__ cmds, int k,
+                                              const VolDev* __restrict__ vols, const PrimCam& C,
+                                              PrimInst* __restrict__ out, int* rtx0, int* rty0, int* rtx1,
+                                              int* rty1);
+
+// Per instance: inverse, local camera, screen-tile rectangle and its tile
+// count (pair_count, scanned for the list fill); per tile: instances listed.
 __global__ void k_prim_prep(const vxl_voxcmd* __restrict__ cmds, int n, const VolDev* __restrict__ vols, PrimCam C,
-                            PrimInst* __restrict__ out, int* __restrict__ tile_count) {
+                            PrimInst* __restrict__ out, int* __restrict__ tile_count, int* __restrict__ pair_count) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
+    int tx0 = 0, ty0 = 0, tx1 = -1, ty1 = -1;
+    if (k < n) {
+        prim_prep_one(cmds, k, vols, C, out, &tx0, &ty0, &tx1, &ty1);
+        pair_count[k] = (tx1 >= tx0 && ty1 >= ty0) ? (tx1 - tx0 + 1) * (ty1 - ty0 + 1) : 0;
+    }
+    warp_rects(tx0, ty0, tx1, ty1, C.tiles_x, [&](int, int t) { atomicAdd(&tile_count[t], 1); });
+}
+
+__device__ __forceinline__ void prim_prep_one(const vxl_voxcmd* __restrict__ cmds, int k,
+                                              const VolDev* __restrict__ vols, const PrimCam& C,
+                                              PrimInst* __restrict__ out, int* rtx0, int* rty0, int* rtx1,
+                                              int* rty1) {
     const float* m = cmds[k].world;
     PrimInst P;
     affine_inverse(m, P.ri, P.ti);
@@ -182,14 +219,15 @@ __global__ void k_prim_prep(const vxl_voxcmd* __restrict__ cmds, int n, const Vo
     P.ty1 = ty1;
     P.near = zmin;
     out[k] = P;
-    if (tx0 <= tx1 && ty0 <= ty1)
-        for (int ty = ty0; ty <= ty1; ty++)
-            for (int tx = tx0; tx <= tx1; tx++) atomicAdd(&tile_count[ty * C.tiles_x + tx], 1);
+    *rtx0 = tx0;
+    *rty0 = ty0;
+    *rtx1 = tx1;
+    *rty1 = ty1;
 }
 
-// exclusive scan of the tile counts (one CTA of 1024 threads, any length):
+// exclusive scan by one CTA of 1024 threads, any length:
 // offsets[t] = sum of counts before t; offsets[ntiles] = total
-__global__ void k_prim_scan(const int* __restrict__ counts, int ntiles, int* __restrict__ offsets) {
+__device__ __forceinline__ void cta_scan(const int* __restrict__ counts, int ntiles, int* __restrict__ offsets) {
     __shared__ int warp_sums[32];
     __shared__ int carry;
     if (threadIdx.x == 0) carry = 0;
@@ -223,20 +261,38 @@ __global__ void k_prim_scan(const int* __restrict__ counts, int ntiles, int* __r
     if (threadIdx.x == 0) offsets[ntiles] = carry;
 }
 
+// CTA 0 scans the per-tile counts, CTA 1 the per-instance tile counts
+__global__ void k_prim_scan(const int* __restrict__ tile_count, int ntiles, int* __restrict__ tile_off,
+                            const int* __restrict__ pair_count, int n, int* __restrict__ pair_off) {
+    if (blockIdx.x == 0)
+        cta_scan(tile_count, ntiles, tile_off);
+    else
+        cta_scan(pair_count, n, pair_off);
+}
+
 // entries beyond the list capacity are dropped; k_primary then scans every
 // instance for every tile (exact, slower) and the host grows the lists
 __global__ void k_prim_fill(const PrimInst* __restrict__ insts, int n, int tiles_x, const int* __restrict__ offsets,
-                            int* __restrict__ cursor, int* __restrict__ lists, int64_t cap) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const PrimInst& P = insts[k];
-    if (P.tx0 > P.tx1 || P.ty0 > P.ty1) return;
-    for (int ty = P.ty0; ty <= P.ty1; ty++)
-        for (int tx = P.tx0; tx <= P.tx1; tx++) {
-            const int t = ty * tiles_x + tx;
-            const int64_t at = (int64_t)offsets[t] + atomicAdd(&cursor[t], 1);
-            if (at < cap) lists[at] = k;
+                            int* __restrict__ cursor, int* __restrict__ lists, int64_t cap,
+                            const int* __restrict__ pair_off) {
+    // every (instance, tile) pair of the frame, spread evenly over the grid:
+    // pair e belongs to the instance k with pair_off[k] <= e < pair_off[k + 1]
+    const int total = pair_off[n];
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        int lo = 0, hi = n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(pair_off + mid) <= e)
+                lo = mid;
+            else
+                hi = mid - 1;
         }
+        const PrimInst& P = insts[lo];
+        const int w = P.tx1 - P.tx0 + 1, q = e - __ldg(pair_off + lo);
+        const int t = (P.ty0 + q / w) * tiles_x + P.tx0 + q % w;
+        const int64_t at = (int64_t)offsets[t] + atomicAdd(&cursor[t], 1);
+        if (at < cap) lists[at] = lo;
+    }
 }
 
 // clipToAABB, GeometryVoxel.frag:50-61
@@ -498,7 +554,8 @@ vxl_status launch_trace_primary(vxl_ctx* ctx, const vxl_volume* volumes, int nvo
     const size_t b_cmd = al(sizeof(vxl_voxcmd) * (size_t)(n > 0 ? n : 1));
     const size_t b_ins = al(sizeof(PrimInst) * (size_t)(n > 0 ? n : 1));
     const size_t b_cnt = al(sizeof(int) * (size_t)(ntiles + 1));
-    const size_t head = b_vol + b_cmd + b_ins + 3 * b_cnt;
+    const size_t b_pc = al(sizeof(int) * (size_t)(n + 1));
+    const size_t head = b_vol + b_cmd + b_ins + 3 * b_cnt + 2 * b_pc;
     void* p;
     VXL_TRY(ctx_scratch(ctx, head, &p));
     char* base = (char*)p;
@@ -508,6 +565,8 @@ vxl_status launch_trace_primary(vxl_ctx* ctx, const vxl_volume* volumes, int nvo
     int* d_count = (int*)(base + b_vol + b_cmd + b_ins);
     int* d_off = (int*)(base + b_vol + b_cmd + b_ins + b_cnt);
     int* d_cur = (int*)(base + b_vol + b_cmd + b_ins + 2 * b_cnt);
+    int* d_pcount = (int*)(base + b_vol + b_cmd + b_ins + 3 * b_cnt);
+    int* d_poff = (int*)(base + b_vol + b_cmd + b_ins + 3 * b_cnt + b_pc);
     std::vector<VolDev> hv((size_t)(nvol > 0 ? nvol : 1));
     for (int v = 0; v < nvol; v++) {
         hv[v].m[0] = volumes[v].mip[0];
@@ -559,10 +618,10 @@ vxl_status launch_trace_primary(vxl_ctx* ctx, const vxl_volume* volumes, int nvo
     VXL_TRY_CUDA(cudaMemsetAsync(d_count, 0, sizeof(int) * (size_t)(ntiles + 1), s));
     VXL_TRY_CUDA(cudaMemsetAsync(d_cur, 0, sizeof(int) * (size_t)(ntiles + 1), s));
     if (n > 0) {
-        k_prim_prep<<<blocks_of((size_t)n, 128), 128, 0, s>>>(d_cmd, n, d_vol, C, d_ins, d_count);
+        k_prim_prep<<<blocks_of((size_t)n, 32), 32, 0, s>>>(d_cmd, n, d_vol, C, d_ins, d_count, d_pcount);
         ctx->launches++;
     }
-    k_prim_scan<<<1, 1024, 0, s>>>(d_count, ntiles, d_off);
+    k_prim_scan<<<n > 0 ? 2 : 1, 1024, 0, s>>>(d_count, ntiles, d_off, d_pcount, n, d_poff);
     ctx->launches++;
     VXL_TRY_CUDA(cudaGetLastError());
     // the list length goes back to the host without a wait; it sizes the next frame's lists
@@ -570,7 +629,8 @@ vxl_status launch_trace_primary(vxl_ctx* ctx, const vxl_volume* volumes, int nvo
     VXL_TRY_CUDA(cudaEventRecord(ctx->pev, s));
     const int64_t cap = (int64_t)ctx->plist_cap;
     if (n > 0) {
-        k_prim_fill<<<blocks_of((size_t)n, 128), 128, 0, s>>>(d_ins, n, C.tiles_x, d_off, d_cur, ctx->d_plist, cap);
+        k_prim_fill<<<(unsigned)ctx->sm_count * 4, 256, 0, s>>>(d_ins, n, C.tiles_x, d_off, d_cur, ctx->d_plist, cap,
+                                                               d_poff);
         ctx->launches++;
     }
     k_primary<<<ntiles, kPrimTile * kPrimTile, 0, s>>>(d_ins, d_vol, C, d_off, ctx->d_plist, cap, n, out->pos,

@@ -847,6 +847,12 @@ vxl_status vxl_trace_primary(vxl_ctx* ctx, const vxl_volume* volumes, int nvolum
     if (cam->width < 1 || cam->height < 1 || (int64_t)cam->width * cam->height > (int64_t)INT32_MAX / 4)
         return fail(VXL_ERR_INVALID_ARG, "trace_primary: bad image size");
     if (!out->pos || !out->nrm) return fail(VXL_ERR_INVALID_ARG, "trace_primary: pos and nrm are required");
+    {  // the screen-tile lists hold at most ncmds x tiles entries, counted in 32 bits
+        const int64_t tiles = (int64_t)((cam->width + 15) / 16) * ((cam->height + 15) / 16);
+        if ((int64_t)ncmds * tiles > (int64_t)INT32_MAX)
+            return fail(VXL_ERR_INVALID_ARG, "trace_primary: %d commands x %lld screen tiles exceed 2^31 list entries",
+                        ncmds, (long long)tiles);
+    }
     for (int v = 0; v < nvolumes; v++) {
         const vxl_volume& V = volumes[v];
         if (!V.mip[0] || !V.mip[1] || !V.mip[2] || V.sx < 4 || V.sy < 4 || V.sz < 4 || V.sx > 32768 ||
