@@ -225,18 +225,26 @@ __device__ __forceinline__ void prim_prep_one(const vxl_voxcmd* __restrict__ cmd
     *rty1 = ty1;
 }
 
-// exclusive scan by one CTA of 1024 threads, any length:
+// exclusive scan by one CTA of 1024 threads, any length, 8 consecutive
+// elements per thread (8192 per pass: one pass for a 1080p frame's tiles):
 // offsets[t] = sum of counts before t; offsets[ntiles] = total
+constexpr int kScanItems = 8;
 __device__ __forceinline__ void cta_scan(const int* __restrict__ counts, int ntiles, int* __restrict__ offsets) {
     __shared__ int warp_sums[32];
     __shared__ int carry;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int base = 0; base < ntiles; base += 1024) {
-        const int i = base + threadIdx.x;
-        const int v = i < ntiles ? counts[i] : 0;
-        int x = v;
+    for (int base = 0; base < ntiles; base += 1024 * kScanItems) {
+        const int i0 = base + threadIdx.x * kScanItems;
+        int v[kScanItems];
+        int x = 0;
+#pragma unroll
+        for (int j = 0; j < kScanItems; j++) {
+            v[j] = i0 + j < ntiles ? counts[i0 + j] : 0;
+            x += v[j];
+        }
+        const int own = x;
         for (int o = 1; o < 32; o <<= 1) {
             const int y = __shfl_up_sync(0xffffffffu, x, o);
             if (lane >= o) x += y;
@@ -252,10 +260,14 @@ __device__ __forceinline__ void cta_scan(const int* __restrict__ counts, int nti
             warp_sums[lane] = w;
         }
         __syncthreads();
-        const int before = (warp > 0 ? warp_sums[warp - 1] : 0) + carry;
-        if (i < ntiles) offsets[i] = before + x - v;
+        int run = (warp > 0 ? warp_sums[warp - 1] : 0) + carry + x - own;
+#pragma unroll
+        for (int j = 0; j < kScanItems; j++) {
+            if (i0 + j < ntiles) offsets[i0 + j] = run;
+            run += v[j];
+        }
         __syncthreads();
-        if (threadIdx.x == 1023) carry = before + x;
+        if (threadIdx.x == 1023) carry = run;
         __syncthreads();
     }
     if (threadIdx.x == 0) offsets[ntiles] = carry;
