@@ -188,6 +188,32 @@ typedef struct vxl_outputs {
 vxl_status vxl_trace_occlusion(vxl_ctx* ctx, const vxl_grid* grid, const vxl_gbuffer* gbuf,
                                const vxl_trace_params* params, const vxl_outputs* out, void* stream);
 
+/* The two ViewBuffer matrices a light pass reads to place a pixel (ViewData,
+ * Sources/Graphics/Renderer/View.h:16-31; Common.frag:45-71), column-major as
+ * glm stores them. */
+typedef struct vxl_view {
+    float inverse_view[16];        /* InverseViewMatrix */
+    float inverse_projection[16];  /* InverseProjectionMatrix */
+} vxl_view;
+
+/* vxl_trace_occlusion with the surface positions rebuilt from the G-buffer's
+ * linear depth the way LightAmbient places a pixel (LightAmbient.vert:32-36,
+ * LightAmbient.frag:136-150), replacing the pass's own G-buffer reads. For
+ * texel (i, j) of a width x height image (row j, row 0 first in memory):
+ *   ndc    = ((i + 0.5)*2/width - 1, 1 - (j + 0.5)*2/height)   (the pass's flipped UV)
+ *   farvec = (inverse_projection * (ndc, 1, 1)).xyz / w
+ *   pos    = farvec * (depth * (1 + 1/4096))                    (FAR = 4096)
+ *   wcp    = (inverse_view * (pos, 1)).xyz * 10                 (fine-voxel units)
+ * each product adding the column terms in column order, fp32, no FMA.
+ * Texels with !(depth < 0.999) are sky: outputs as for a zero normal.
+ * d_depth: float[height][width], (w - NEAR)/(FAR - NEAR) as GeometryVoxel.frag:169
+ * writes it; d_nrm: float[height*width][3] world normals; d_rough optional.
+ * Outputs per texel. Uses a context workspace of 24 bytes per texel. */
+vxl_status vxl_trace_occlusion_from_depth(vxl_ctx* ctx, const vxl_grid* grid, const float* d_depth,
+                                          const float* d_nrm, const float* d_rough, int32_t width, int32_t height,
+                                          const vxl_view* view, const vxl_trace_params* params,
+                                          const vxl_outputs* out, void* stream);
+
 /* Same, with the G-buffer held in host memory (pinned or pageable): the
  * library copies it in through its context staging buffers, traces, and
  * copies the outputs back to host memory. Synchronous on `stream`. Host

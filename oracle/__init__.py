@@ -144,6 +144,7 @@ def lib():
                                             C.c_float, C.c_float, C.c_float, C.c_int, C.c_int, fp, fp,
                                             C.POINTER(C.c_uint32), ip]
             L.vo_affine_inverse.argtypes = [fp, fp, fp]
+            L.vo_rebuild_from_depth.argtypes = [fp, fp, C.c_int, C.c_int, fp, fp, fp, fp]
             L.vo_primary.argtypes = [vp, vp, vp, ip, fp, ip, C.c_int, fp, fp, C.c_float, C.c_int, C.c_int, C.c_int,
                                      fp, fp, fp, ip, ip, C.c_int]
             L.vo_taa.argtypes = [fp, fp, fp, fp, fp, fp, fp, fp, C.c_int, C.c_int, fp, C.c_int]
@@ -474,6 +475,20 @@ def affine_inverse(m16):
     ti = np.zeros(3, np.float32)
     lib().vo_affine_inverse(_f(m), _f(ri), _f(ti))
     return ri, ti
+
+
+def rebuild_from_depth(depth, nrm, W, H, inv_view, inv_proj):
+    """Fine-unit surface positions and sky-masked normals from a linear-depth
+    G-buffer, as LightAmbient places a pixel (vo_rebuild_from_depth)."""
+    depth = np.ascontiguousarray(depth, np.float32).reshape(-1)
+    nrm = np.ascontiguousarray(nrm, np.float32).reshape(-1, 3)
+    iv = np.ascontiguousarray(inv_view, np.float32).reshape(16)
+    ip = np.ascontiguousarray(inv_proj, np.float32).reshape(16)
+    assert depth.shape[0] == W * H and nrm.shape[0] == W * H
+    wcp = np.zeros((W * H, 3), np.float32)
+    n2 = np.zeros((W * H, 3), np.float32)
+    lib().vo_rebuild_from_depth(_f(depth), _f(nrm), W, H, _f(iv), _f(ip), _f(wcp), _f(n2))
+    return wcp, n2
 
 
 def primary(volumes, worlds, vol_of, cam, target, W, H, frame=0, tan_half_fov=0.57735026, threads=None):

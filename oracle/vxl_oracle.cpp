@@ -1544,3 +1544,53 @@ extern "C" void vo_taa(const float* light, const float* last, const float* color
         taa_pixel(I, noise + 4 * (size_t)i, i % W, i / W, out + 4 * (size_t)i);
     });
 }
+
+// ------------------------------------------------------------ depth -> position
+// LightAmbient.vert:32-36: FarVec = (InverseProjection * (Pos.xy, 1, 1)).xyz / w at
+// the full-screen pass's vertices, interpolated; it is linear in Pos.xy (a
+// perspective inverse has a constant w at z = 1), so it is evaluated here at
+// the fragment's NDC. The pass samples the G-buffer at UV = (Pos.xy*0.5+0.5)
+// with UV.y flipped (:40-41), so texel (i, j) -- row j from the start of the
+// image -- is read by the fragment at NDC ((i+0.5)*2/W - 1, 1 - (j+0.5)*2/H).
+// LightAmbient.frag:141: pos = FarVec * (depth * (1 + 1/FAR)), FAR = 4096;
+// :150: wcp = (InverseView * (pos, 1)).xyz * 10. Sky: !(depth < 0.999) (:138).
+// Matrix-vector products add the column terms in column order, fp32, no FMA.
+static void mat4_vec(const float* m, float x, float y, float z, float w, float* o) {
+    for (int r = 0; r < 4; r++) {
+        float a = m[r] * x;
+        a = a + m[4 + r] * y;
+        a = a + m[8 + r] * z;
+        a = a + m[12 + r] * w;
+        o[r] = a;
+    }
+}
+
+void vo_rebuild_from_depth(const float* depth, const float* nrm, int W, int H, const float* inv_view,
+                           const float* inv_proj, float* wcp, float* nrm_out) {
+    const float kFarScale = 1.0f + 1.0f / 4096.0f;
+    for (int j = 0; j < H; j++)
+        for (int i = 0; i < W; i++) {
+            const size_t k = (size_t)j * W + i;
+            const float d = depth[k];
+            float* p = wcp + 3 * k;
+            float* n = nrm_out + 3 * k;
+            if (!(d < 0.999f)) {
+                p[0] = p[1] = p[2] = 0.0f;
+                n[0] = n[1] = n[2] = 0.0f;
+                continue;
+            }
+            const float nx = ((float)i + 0.5f) * 2.0f / (float)W - 1.0f;
+            const float ny = 1.0f - ((float)j + 0.5f) * 2.0f / (float)H;
+            float v[4], q[4];
+            mat4_vec(inv_proj, nx, ny, 1.0f, 1.0f, v);
+            const float s = d * kFarScale;
+            const float px = (v[0] / v[3]) * s, py = (v[1] / v[3]) * s, pz = (v[2] / v[3]) * s;
+            mat4_vec(inv_view, px, py, pz, 1.0f, q);
+            p[0] = q[0] * 10.0f;
+            p[1] = q[1] * 10.0f;
+            p[2] = q[2] * 10.0f;
+            n[0] = nrm[3 * k];
+            n[1] = nrm[3 * k + 1];
+            n[2] = nrm[3 * k + 2];
+        }
+}

@@ -162,6 +162,13 @@ void vo_primary(const uint8_t* const* mip0s, const uint8_t* const* mip1s, const 
                 const float* target, float tan_half_fov, int W, int H, int frame, float* pos, float* nrm,
                 float* depth, int32_t* material, int32_t* instance, int threads);
 
+/* Surface position from the G-buffer's linear depth, as LightAmbient places a
+ * pixel (LightAmbient.vert:32-36 FarVec with the pass's flipped UV;
+ * LightAmbient.frag:138-150): wcp[npix][3] in fine units, nrm_out = nrm, or 0
+ * for sky texels (!(depth < 0.999)). Matrices column-major. */
+void vo_rebuild_from_depth(const float* depth, const float* nrm, int W, int H, const float* inv_view,
+                           const float* inv_proj, float* wcp, float* nrm_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -33,6 +33,15 @@ def test_every_declared_symbol_is_exported(V):
     assert sorted(V.EXPORTED) == names
 
 
+def test_binding_declares_every_argument_list(V):
+    """ctypes passes an undeclared argument as a C int: a 64-bit device pointer
+    would be cut to 32 bits. Every entry point that takes arguments declares them."""
+    L = V.lib()
+    no_args = {"vxl_abi_version", "vxl_last_error_string"}
+    undeclared = [n for n in V.EXPORTED if n not in no_args and getattr(L, n).argtypes is None]
+    assert not undeclared, undeclared
+
+
 def test_abi_version_and_status_strings(V):
     L = V.lib()
     assert L.vxl_abi_version() == 1

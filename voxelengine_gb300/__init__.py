@@ -36,7 +36,8 @@ EXPORTED = [
     "vxl_abi_version", "vxl_last_error_string", "vxl_status_string", "vxl_ctx_create", "vxl_ctx_destroy",
     "vxl_ctx_launch_count", "vxl_ctx_set_tuning", "vxl_ctx_get_tuning", "vxl_grid_create", "vxl_grid_destroy", "vxl_grid_describe", "vxl_grid_clear",
     "vxl_grid_build_bricks", "vxl_grid_import_r8", "vxl_grid_export_r8", "vxl_grid_import_palette",
-    "vxl_grid_count", "vxl_trace_rays", "vxl_trace_occlusion", "vxl_trace_occlusion_host", "vxl_batch_create",
+    "vxl_grid_count", "vxl_trace_rays", "vxl_trace_occlusion", "vxl_trace_occlusion_host",
+    "vxl_trace_occlusion_from_depth", "vxl_batch_create",
     "vxl_batch_run", "vxl_batch_destroy", "vxl_batch_info", "vxl_light_ambient",
     "vxl_light_reflection", "vxl_light_point", "vxl_light_points", "vxl_light_taa", "vxl_voxelize", "vxl_voxelize_noalloc", "vxl_shadowvox_update",
     "vxl_vox_destroyed",
@@ -118,6 +119,10 @@ class TaaFrame(C.Structure):
                 ("width", C.c_int32), ("height", C.c_int32)]
 
 
+class View(C.Structure):
+    _fields_ = [("inverse_view", C.c_float * 16), ("inverse_projection", C.c_float * 16)]
+
+
 class Light(C.Structure):
     _fields_ = [("pos", C.c_float * 3), ("range", C.c_float), ("spot", C.c_int32), ("pad", C.c_int32 * 3)]
 
@@ -181,6 +186,8 @@ def lib():
         L.vxl_trace_rays.argtypes = [vp, vp, vp, i64, C.c_int, vp, vp]
         L.vxl_trace_occlusion.argtypes = [vp, vp, C.POINTER(GBuffer), C.POINTER(TraceParams), C.POINTER(Outputs), vp]
         L.vxl_trace_occlusion_host.argtypes = [vp, vp, vp, vp, vp, i64, C.POINTER(TraceParams), vp, vp, vp, vp, vp, vp]
+        L.vxl_trace_occlusion_from_depth.argtypes = [vp, vp, vp, vp, vp, C.c_int32, C.c_int32, C.POINTER(View),
+                                                     C.POINTER(TraceParams), C.POINTER(Outputs), vp]
         L.vxl_batch_create.argtypes = [vp, C.POINTER(BatchItem), C.c_int, C.c_int, C.POINTER(vp)]
         L.vxl_batch_run.argtypes = [vp, vp]
         L.vxl_batch_destroy.argtypes = [vp]
@@ -382,6 +389,20 @@ def trace_occlusion(ctx: Context, grid: Grid, pos, nrm, rough, npix: int, params
     out = Outputs(_ptr(shadow), _ptr(ao), _ptr(ao_vis), _ptr(spec), _ptr(spec_t), _ptr(records))
     check(lib().vxl_trace_occlusion(ctx.handle, grid.handle, C.byref(gb), C.byref(params), C.byref(out),
                                     _stream(stream)))
+
+
+def trace_occlusion_from_depth(ctx: Context, grid: Grid, depth, nrm, rough, W: int, H: int, inv_view, inv_proj,
+                               params: TraceParams, shadow=None, ao=None, ao_vis=None, spec=None, spec_t=None,
+                               records=None, stream=None):
+    """vxl_trace_occlusion_from_depth: positions rebuilt from a linear-depth
+    G-buffer as LightAmbient places a pixel; inv_view / inv_proj are the view
+    buffer's InverseViewMatrix / InverseProjectionMatrix (column-major 16 floats)."""
+    v = View()
+    v.inverse_view[:] = [float(x) for x in np.asarray(inv_view, np.float32).reshape(16)]
+    v.inverse_projection[:] = [float(x) for x in np.asarray(inv_proj, np.float32).reshape(16)]
+    out = Outputs(_ptr(shadow), _ptr(ao), _ptr(ao_vis), _ptr(spec), _ptr(spec_t), _ptr(records))
+    check(lib().vxl_trace_occlusion_from_depth(ctx.handle, grid.handle, _ptr(depth), _ptr(nrm), _ptr(rough), W, H,
+                                               C.byref(v), C.byref(params), C.byref(out), _stream(stream)))
 
 
 def trace_occlusion_host(ctx: Context, grid: Grid, h_pos, h_nrm, h_rough, npix: int, params: TraceParams,

@@ -444,4 +444,66 @@ vxl_status launch_scene_gbuffer(const vxl_grid* g, const float cam[3], const flo
     return VXL_OK;
 }
 
+// Surface positions from a linear-depth G-buffer as LightAmbient places a
+// pixel (LightAmbient.vert:32-36, LightAmbient.frag:136-150); the oracle's
+// vo_rebuild_from_depth is the same arithmetic in the same order.
+struct ViewMats {
+    float iv[16], ip[16];
+};
+
+__device__ __forceinline__ void mat4_vec(const float* m, float x, float y, float z, float w, float* o) {
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        float a = m[r] * x;
+        a = a + m[4 + r] * y;
+        a = a + m[8 + r] * z;
+        a = a + m[12 + r] * w;
+        o[r] = a;
+    }
+}
+
+__global__ void k_rebuild_from_depth(const float* __restrict__ depth, const float* __restrict__ nrm, int W, int H,
+                                     const ViewMats M, float* __restrict__ wcp, float* __restrict__ nrm_out) {
+    const int64_t n = (int64_t)W * H;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(k % W), j = (int)(k / W);
+        const float d = depth[k];
+        float* p = wcp + 3 * k;
+        float* o = nrm_out + 3 * k;
+        if (!(d < 0.999f)) {
+            p[0] = p[1] = p[2] = 0.0f;
+            o[0] = o[1] = o[2] = 0.0f;
+            continue;
+        }
+        const float nx = ((float)i + 0.5f) * 2.0f / (float)W - 1.0f;
+        const float ny = 1.0f - ((float)j + 0.5f) * 2.0f / (float)H;
+        float v[4], q[4];
+        mat4_vec(M.ip, nx, ny, 1.0f, 1.0f, v);
+        const float s = d * (1.0f + 1.0f / 4096.0f);
+        const float px = (v[0] / v[3]) * s, py = (v[1] / v[3]) * s, pz = (v[2] / v[3]) * s;
+        mat4_vec(M.iv, px, py, pz, 1.0f, q);
+        p[0] = q[0] * 10.0f;
+        p[1] = q[1] * 10.0f;
+        p[2] = q[2] * 10.0f;
+        o[0] = nrm[3 * k];
+        o[1] = nrm[3 * k + 1];
+        o[2] = nrm[3 * k + 2];
+    }
+}
+
+vxl_status launch_rebuild_from_depth(vxl_ctx* ctx, const float* depth, const float* nrm, int W, int H,
+                                     const vxl_view* view, float* wcp, float* nrm_out, cudaStream_t s) {
+    ViewMats M;
+    for (int k = 0; k < 16; k++) {
+        M.iv[k] = view->inverse_view[k];
+        M.ip[k] = view->inverse_projection[k];
+    }
+    const int64_t n = (int64_t)W * H;
+    const unsigned blocks = (unsigned)std::min<int64_t>((n + 255) / 256, (int64_t)ctx->sm_count * 16);
+    k_rebuild_from_depth<<<blocks, 256, 0, s>>>(depth, nrm, W, H, M, wcp, nrm_out);
+    ctx->launches++;
+    VXL_TRY_CUDA(cudaGetLastError());
+    return VXL_OK;
+}
+
 }  // namespace vxl

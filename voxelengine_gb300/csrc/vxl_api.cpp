@@ -225,6 +225,7 @@ vxl_status vxl_ctx_destroy(vxl_ctx* ctx) {
     if (ctx->h_ptotal) cudaFreeHost(ctx->h_ptotal);
     if (ctx->h_pin) cudaFreeHost(ctx->h_pin);
     if (ctx->d_taa) cudaFree(ctx->d_taa);
+    if (ctx->d_fd) cudaFree(ctx->d_fd);
     delete ctx;
     return VXL_OK;
 }
@@ -408,6 +409,25 @@ vxl_status vxl_trace_occlusion(vxl_ctx* ctx, const vxl_grid* g, const vxl_gbuffe
     if (gb->npix > 0 && (!gb->pos || !gb->nrm)) return fail(VXL_ERR_INVALID_ARG, "trace_occlusion: NULL G-buffer");
     VXL_TRY(set_device(ctx));
     return launch_trace_occlusion(ctx, g, gb, p, out, (cudaStream_t)stream);
+}
+
+vxl_status vxl_trace_occlusion_from_depth(vxl_ctx* ctx, const vxl_grid* g, const float* d_depth, const float* d_nrm,
+                                          const float* d_rough, int32_t width, int32_t height, const vxl_view* view,
+                                          const vxl_trace_params* p, const vxl_outputs* out, void* stream) {
+    if (!ctx || !grid_ok(g) || !view || !out) return fail(VXL_ERR_INVALID_ARG, "trace_occlusion_from_depth: NULL argument");
+    VXL_TRY(check_params(p));
+    if (width < 0 || height < 0) return fail(VXL_ERR_INVALID_ARG, "trace_occlusion_from_depth: bad image size");
+    const int64_t npix = (int64_t)width * height;
+    if (npix == 0) return VXL_OK;
+    if (!d_depth || !d_nrm) return fail(VXL_ERR_INVALID_ARG, "trace_occlusion_from_depth: NULL G-buffer");
+    VXL_TRY(set_device(ctx));
+    cudaStream_t s = (cudaStream_t)stream;
+    VXL_TRY(ctx_grow(&ctx->d_fd, &ctx->fd_bytes, (size_t)npix * 6 * sizeof(float)));
+    float* wcp = (float*)ctx->d_fd;
+    float* nrm = wcp + 3 * npix;
+    VXL_TRY(launch_rebuild_from_depth(ctx, d_depth, d_nrm, width, height, view, wcp, nrm, s));
+    const vxl_gbuffer gb{wcp, nrm, d_rough, npix, width, height};
+    return launch_trace_occlusion(ctx, g, &gb, p, out, s);
 }
 
 vxl_status vxl_trace_occlusion_host(vxl_ctx* ctx, const vxl_grid* g, const float* h_pos, const float* h_nrm,

@@ -39,6 +39,9 @@ struct vxl_ctx {
     // temporal accumulation: the per-texel records the spiral taps read
     void* d_taa;
     size_t taa_bytes;
+    // positions and sky-masked normals rebuilt from a depth G-buffer
+    void* d_fd;
+    size_t fd_bytes;
 };
 constexpr uint32_t kCounterRing = 4096;
 
@@ -98,6 +101,8 @@ vxl_status launch_scene_boxes(vxl_grid* g, uint32_t seed, int nboxes, int smin, 
 vxl_status launch_scene_terrain(vxl_grid* g, uint32_t seed, float base, float amp, float freq, int octaves,
                                 float* d_height, cudaStream_t s);
 vxl_status launch_light_taa(vxl_ctx* ctx, const vxl_taa_frame* f, float* out, cudaStream_t s);
+vxl_status launch_rebuild_from_depth(vxl_ctx* ctx, const float* depth, const float* nrm, int W, int H,
+                                     const vxl_view* view, float* wcp, float* nrm_out, cudaStream_t s);
 vxl_status launch_light_points(vxl_ctx* ctx, const vxl_grid* g, const float* wpos, const float* nrm,
                                const float* noise, int64_t npix, const vxl_light* lights, int nlights,
                                unsigned long long* lit, unsigned long long* in_range, cudaStream_t s);
