@@ -396,6 +396,11 @@ def run_gpu(args, wl):
         line["cpu_baseline"] = {"value": v / 1e9, "unit": "Grays/s", "cores": th, "kind": "port",
                                 "sample": "%d whole image rows of %d in seeded random order (%.1f s), %d rays/px" % (
                                     rows, H, dt, R)}
+        v1, rows1, dt1, _ = cpu_sample_rays_per_s(g_np, pos.cpu().numpy(), nrm.cpu().numpy(),
+                                                  rough.cpu().numpy(), OP, W, H,
+                                                  budget_s=min(4.0, args.cpu_seconds), threads=1)
+        line["cpu_baseline"]["one_core"] = {"value": v1 / 1e9, "unit": "Grays/s", "cores": 1,
+                                            "sample": "%d whole image rows (%.1f s)" % (rows1, dt1)}
     print(json.dumps(line))
 
 
