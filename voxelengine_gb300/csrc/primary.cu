@@ -339,13 +339,16 @@ __device__ __forceinline__ bool intersect_volume(const VolDev& V, f3 origin, f3 
     int i = 0;
     do {
         const float mipSize = (float)(1 << mip);
-        origin = mk(origin.x / mipSize, origin.y / mipSize, origin.z / mipSize);
+        // x / mipSize for mipSize = 1, 2, 4: the exact reciprocal times x rounds the
+        // same real value, so the multiply gives the division's float
+        const float invMip = mip == 2 ? 0.25f : (mip == 1 ? 0.5f : 1.0f);
+        origin = mk(origin.x * invMip, origin.y * invMip, origin.z * invMip);
         int cx = (int)floorf(origin.x), cy = (int)floorf(origin.y), cz = (int)floorf(origin.z);
         const f3 nb = mk((float)cx + (ss.x * 0.5f + 0.5f), (float)cy + (ss.y * 0.5f + 0.5f),
                          (float)cz + (ss.z * 0.5f + 0.5f));
         f3 tm = mk((nb.x - origin.x) / direction.x, (nb.y - origin.y) / direction.y, (nb.z - origin.z) / direction.z);
-        const int ux = (int)((float)V.sx / mipSize) + 1, uy = (int)((float)V.sy / mipSize) + 1,
-                  uz = (int)((float)V.sz / mipSize) + 1;
+        const int ux = (int)((float)V.sx * invMip) + 1, uy = (int)((float)V.sy * invMip) + 1,
+                  uz = (int)((float)V.sz * invMip) + 1;
         int n = 0;
         do {
             const float selx = glsl_step(tm.x, tm.z) * glsl_step(tm.x, tm.y);
@@ -377,7 +380,7 @@ __device__ __forceinline__ bool intersect_volume(const VolDev& V, f3 origin, f3 
                 } else {
                     mip--;
                     const f3 st = mul(direction, best_t);
-                    origin = add(origin, mk(st.x / mipSize, st.y / mipSize, st.z / mipSize));
+                    origin = add(origin, mk(st.x * invMip, st.y * invMip, st.z * invMip));
                     break;
                 }
             }
