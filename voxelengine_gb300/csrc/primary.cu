@@ -308,10 +308,10 @@ __global__ void k_prim_fill(const PrimInst* __restrict__ insts, int n, int tiles
 }
 
 // clipToAABB, GeometryVoxel.frag:50-61
-__device__ __forceinline__ f3 clip_to_aabb(f3 o, f3 d, f3 size) {
+// (inv = 1 / d per component, computed once by the caller)
+__device__ __forceinline__ f3 clip_to_aabb(f3 o, f3 d, f3 inv, f3 size) {
     const f3 c = mk(gmin(gmax(o.x, 0.0f), size.x), gmin(gmax(o.y, 0.0f), size.y), gmin(gmax(o.z, 0.0f), size.z));
     if (c.x == o.x && c.y == o.y && c.z == o.z) return o;
-    const f3 inv = mk(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
     const f3 sgn = mk(glsl_step(d.x, 0.0f), glsl_step(d.y, 0.0f), glsl_step(d.z, 0.0f));
     const f3 t = mk((sgn.x * size.x - o.x) * inv.x, (sgn.y * size.y - o.y) * inv.y, (sgn.z * size.z - o.z) * inv.z);
     const float tmin = gmax(gmax(t.x, t.y), t.z);
@@ -329,12 +329,26 @@ __device__ __forceinline__ uint32_t vol_texel(const VolDev& V, int mip, int x, i
     return __ldg(m + ((size_t)x + (size_t)y * sx + (size_t)z * sx * sy));
 }
 
+// 1 / (d * sign(d)) from inv = 1 / d: for d != 0, d * sign(d) = |d| exactly and
+// IEEE division is symmetric in sign, so the quotient is |inv|; for d = +-0,
+// sign(d) = +0 and the quotient is an infinity with the sign of d * +0
+// (a NaN d gives the canonical NaN either way)
+__device__ __forceinline__ float abs_recip(float d, float sgn, float inv) {
+    const float a = d * sgn;
+    return a == 0.0f ? __int_as_float(0x7f800000 | (__float_as_int(a) & 0x80000000)) : fabsf(inv);
+}
+
 // intersectVolume, GeometryVoxel.frag:63-125 (LOD 1, MIP_COUNT 2,
-// TRANSPARENCY 1), operation for operation
-__device__ __forceinline__ bool intersect_volume(const VolDev& V, f3 origin, f3 direction, f3 lcam, float uvx, float uvy, float resx,
-                                 float resy, int frame, f3* hit, f3* normal, uint32_t* material) {
+// TRANSPARENCY 1), operation for operation (inv = 1 / direction)
+__device__ __forceinline__ bool intersect_volume(const VolDev& V, f3 origin, f3 direction, f3 inv, f3 lcam, float uvx,
+                                                 float uvy, float resx, float resy, int frame, f3* hit, f3* normal,
+                                                 uint32_t* material) {
     const f3 ss = mk(glsl_sign(direction.x), glsl_sign(direction.y), glsl_sign(direction.z));
-    const f3 td = mk(1.0f / (direction.x * ss.x), 1.0f / (direction.y * ss.y), 1.0f / (direction.z * ss.z));
+    const f3 td = mk(abs_recip(direction.x, ss.x, inv.x), abs_recip(direction.y, ss.y, inv.y),
+                     abs_recip(direction.z, ss.z, inv.z));
+    // int(select * sign) with select in {0, 1} and sign in {-1, 0, 1}: the
+    // integer sign where the axis is selected
+    const int isx = (int)ss.x, isy = (int)ss.y, isz = (int)ss.z;
     int mip = 2;
     int i = 0;
     do {
@@ -354,9 +368,9 @@ __device__ __forceinline__ bool intersect_volume(const VolDev& V, f3 origin, f3 
             const float selx = glsl_step(tm.x, tm.z) * glsl_step(tm.x, tm.y);
             const float sely = glsl_step(tm.y, tm.x) * glsl_step(tm.y, tm.z);
             const float selz = glsl_step(tm.z, tm.y) * glsl_step(tm.z, tm.x);
-            cx += (int)(selx * ss.x);
-            cy += (int)(sely * ss.y);
-            cz += (int)(selz * ss.z);
+            cx += selx != 0.0f ? isx : 0;
+            cy += sely != 0.0f ? isy : 0;
+            cz += selz != 0.0f ? isz : 0;
             if (cx < -1 || cy < -1 || cz < -1 || cx > ux || cy > uy || cz > uz) return false;
             const uint32_t voxel = vol_texel(V, mip, cx, cy, cz);
             if (voxel != 0u) {
@@ -462,20 +476,20 @@ __global__ void __launch_bounds__(256, 3) k_primary(const PrimInst* __restrict__
                 const f3 ld = normalize(rmul3(P.ri, d));
                 // the pixel ray enters the volume box
                 const float dims[3] = {(float)V.sx, (float)V.sy, (float)V.sz};
-                const float lo[3] = {lc.x, lc.y, lc.z}, dl[3] = {ld.x, ld.y, ld.z};
+                const f3 inv = mk(1.0f / ld.x, 1.0f / ld.y, 1.0f / ld.z);
+                const float lo[3] = {lc.x, lc.y, lc.z}, iv[3] = {inv.x, inv.y, inv.z};
                 float t0 = -INFINITY, t1 = INFINITY;
 #pragma unroll
                 for (int a = 0; a < 3; a++) {
-                    const float inv = 1.0f / dl[a];
-                    const float ta = (0.0f - lo[a]) * inv, tb = (dims[a] - lo[a]) * inv;
+                    const float ta = (0.0f - lo[a]) * iv[a], tb = (dims[a] - lo[a]) * iv[a];
                     t0 = fmaxf(t0, fminf(ta, tb));
                     t1 = fminf(t1, fmaxf(ta, tb));
                 }
                 if (!(t0 <= t1 && t1 >= 0.0f)) continue;
-                const f3 o = clip_to_aabb(lc, ld, mk(dims[0], dims[1], dims[2]));
+                const f3 o = clip_to_aabb(lc, ld, inv, mk(dims[0], dims[1], dims[2]));
                 f3 h, nn;
                 uint32_t mat;
-                if (!intersect_volume(V, o, ld, lc, uvx, uvy, (float)C.W, (float)C.H, C.frame, &h, &nn, &mat))
+                if (!intersect_volume(V, o, ld, inv, lc, uvx, uvy, (float)C.W, (float)C.H, C.frame, &h, &nn, &mat))
                     continue;
                 const f3 wl = cmul3(P.M, mul(h, 0.1f));
                 const f3 wp = mk(wl.x + P.M[9], wl.y + P.M[10], wl.z + P.M[11]);
