@@ -318,15 +318,21 @@ __device__ __forceinline__ f3 clip_to_aabb(f3 o, f3 d, f3 inv, f3 size) {
     return add(o, mul(d, tmin - 0.001f));
 }
 
-// texelFetch(VOLUME_TEXTURE, p, mip).r with robust out-of-range = 0 (mip
-// chosen by selects, not array indexing, so the volume stays in registers)
-__device__ __forceinline__ uint32_t vol_texel(const VolDev& V, int mip, int x, int y, int z) {
-    const int sx = mip == 0 ? V.dx[0] : (mip == 1 ? V.dx[1] : V.dx[2]);
-    const int sy = mip == 0 ? V.dy[0] : (mip == 1 ? V.dy[1] : V.dy[2]);
-    const int sz = mip == 0 ? V.dz[0] : (mip == 1 ? V.dz[1] : V.dz[2]);
-    const uint8_t* m = mip == 0 ? V.m[0] : (mip == 1 ? V.m[1] : V.m[2]);
-    if (x < 0 || y < 0 || z < 0 || x >= sx || y >= sy || z >= sz) return 0u;
-    return __ldg(m + ((size_t)x + (size_t)y * sx + (size_t)z * sx * sy));
+// One mip level of a volume: texels and dimensions, loaded from the volume
+// table when the walk enters the level (only the level in use is held in
+// registers)
+struct VolLevel {
+    const uint8_t* m;
+    int sx, sy, sz;
+};
+__device__ __forceinline__ VolLevel vol_level(const VolDev* __restrict__ vp, int mip) {
+    return VolLevel{vp->m[mip], vp->dx[mip], vp->dy[mip], vp->dz[mip]};
+}
+
+// texelFetch(VOLUME_TEXTURE, p, mip).r with robust out-of-range = 0
+__device__ __forceinline__ uint32_t vol_texel(const VolLevel& L, int x, int y, int z) {
+    if (x < 0 || y < 0 || z < 0 || x >= L.sx || y >= L.sy || z >= L.sz) return 0u;
+    return __ldg(L.m + ((size_t)x + (size_t)y * L.sx + (size_t)z * L.sx * L.sy));
 }
 
 // 1 / (d * sign(d)) from inv = 1 / d: for d != 0, d * sign(d) = |d| exactly and
@@ -340,7 +346,7 @@ __device__ __forceinline__ float abs_recip(float d, float sgn, float inv) {
 
 // intersectVolume, GeometryVoxel.frag:63-125 (LOD 1, MIP_COUNT 2,
 // TRANSPARENCY 1), operation for operation (inv = 1 / direction)
-__device__ __forceinline__ bool intersect_volume(const VolDev& V, f3 origin, f3 direction, f3 inv, f3 lcam, float uvx,
+__device__ __forceinline__ bool intersect_volume(const VolDev* __restrict__ vp, f3 origin, f3 direction, f3 inv, f3 lcam, float uvx,
                                                  float uvy, float resx, float resy, int frame, f3* hit, f3* normal,
                                                  uint32_t* material) {
     const f3 ss = mk(glsl_sign(direction.x), glsl_sign(direction.y), glsl_sign(direction.z));
@@ -361,8 +367,9 @@ __device__ __forceinline__ bool intersect_volume(const VolDev& V, f3 origin, f3 
         const f3 nb = mk((float)cx + (ss.x * 0.5f + 0.5f), (float)cy + (ss.y * 0.5f + 0.5f),
                          (float)cz + (ss.z * 0.5f + 0.5f));
         f3 tm = mk((nb.x - origin.x) / direction.x, (nb.y - origin.y) / direction.y, (nb.z - origin.z) / direction.z);
-        const int ux = (int)((float)V.sx * invMip) + 1, uy = (int)((float)V.sy * invMip) + 1,
-                  uz = (int)((float)V.sz * invMip) + 1;
+        const int ux = (int)((float)vp->sx * invMip) + 1, uy = (int)((float)vp->sy * invMip) + 1,
+                  uz = (int)((float)vp->sz * invMip) + 1;
+        const VolLevel L = vol_level(vp, mip);
         int n = 0;
         do {
             const float selx = glsl_step(tm.x, tm.z) * glsl_step(tm.x, tm.y);
@@ -372,7 +379,7 @@ __device__ __forceinline__ bool intersect_volume(const VolDev& V, f3 origin, f3 
             cy += sely != 0.0f ? isy : 0;
             cz += selz != 0.0f ? isz : 0;
             if (cx < -1 || cy < -1 || cz < -1 || cx > ux || cy > uy || cz > uz) return false;
-            const uint32_t voxel = vol_texel(V, mip, cx, cy, cz);
+            const uint32_t voxel = vol_texel(L, cx, cy, cz);
             if (voxel != 0u) {
                 float best_t = tm.x * selx + tm.y * sely;
                 best_t = best_t + tm.z * selz;
@@ -410,7 +417,7 @@ __device__ __forceinline__ bool intersect_volume(const VolDev& V, f3 origin, f3 
 // instances' nearest corner depth; a pixel stops scanning a chunk once that
 // depth, less a safety margin for rounding, is beyond its current hit (no
 // instance further in the chunk can be nearer).
-__global__ void __launch_bounds__(256, 3) k_primary(const PrimInst* __restrict__ insts, const VolDev* __restrict__ vols,
+__global__ void __launch_bounds__(256, 4) k_primary(const PrimInst* __restrict__ insts, const VolDev* __restrict__ vols,
                                                     PrimCam C, const int* __restrict__ offsets,
                                                     const int* __restrict__ lists, int64_t cap, int ninst,
                                                     float* __restrict__ pos, float* __restrict__ nrm,
@@ -471,11 +478,11 @@ __global__ void __launch_bounds__(256, 3) k_primary(const PrimInst* __restrict__
                 if (bi >= 0 && nz - (1e-3f * fabsf(nz) + 1e-3f) > best) break;
                 const int k = s_id[e];
                 const PrimInst& P = insts[k];
-                const VolDev V = vols[P.vol];
+                const VolDev* vp = vols + P.vol;
                 const f3 lc = mk(P.lc[0], P.lc[1], P.lc[2]);
                 const f3 ld = normalize(rmul3(P.ri, d));
                 // the pixel ray enters the volume box
-                const float dims[3] = {(float)V.sx, (float)V.sy, (float)V.sz};
+                const float dims[3] = {(float)vp->sx, (float)vp->sy, (float)vp->sz};
                 const f3 inv = mk(1.0f / ld.x, 1.0f / ld.y, 1.0f / ld.z);
                 const float lo[3] = {lc.x, lc.y, lc.z}, iv[3] = {inv.x, inv.y, inv.z};
                 float t0 = -INFINITY, t1 = INFINITY;
@@ -489,7 +496,7 @@ __global__ void __launch_bounds__(256, 3) k_primary(const PrimInst* __restrict__
                 const f3 o = clip_to_aabb(lc, ld, inv, mk(dims[0], dims[1], dims[2]));
                 f3 h, nn;
                 uint32_t mat;
-                if (!intersect_volume(V, o, ld, inv, lc, uvx, uvy, (float)C.W, (float)C.H, C.frame, &h, &nn, &mat))
+                if (!intersect_volume(vp, o, ld, inv, lc, uvx, uvy, (float)C.W, (float)C.H, C.frame, &h, &nn, &mat))
                     continue;
                 const f3 wl = cmul3(P.M, mul(h, 0.1f));
                 const f3 wp = mk(wl.x + P.M[9], wl.y + P.M[10], wl.z + P.M[11]);
