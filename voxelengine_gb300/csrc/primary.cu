@@ -454,11 +454,14 @@ __global__ void __launch_bounds__(256, 4) k_primary(const PrimInst* __restrict__
             s_near[threadIdx.x] = INFINITY;
         }
         __syncthreads();
-        // bitonic sort of the 256 (near, id) pairs, ascending
-        for (int size = 2; size <= 256; size <<= 1)
+        // bitonic sort of the first n2 (near, id) pairs, ascending: n2 = the power of
+        // two at or above the chunk's length (the padding entries sort last)
+        int n2 = 2;
+        while (n2 < cn) n2 <<= 1;
+        for (int size = 2; size <= n2; size <<= 1)
             for (int stride = size >> 1; stride > 0; stride >>= 1) {
                 const int a = threadIdx.x, b = a ^ stride;
-                if (b > a) {
+                if (b > a && b < n2) {
                     const bool up = (a & size) == 0;
                     const float na = s_near[a], nb = s_near[b];
                     const int ia = s_id[a], ib = s_id[b];
