@@ -152,6 +152,9 @@ extern "C" vxl_status vxl_voxelize_noalloc(const vxl_grid_desc* gd, const vxl_mo
     v.bxy = (uint32_t)gd->bx * (uint32_t)gd->by;
     v.tx = gd->tx;
     v.txy = (uint32_t)gd->tx * (uint32_t)gd->ty;
+    v.ux = (uint32_t)gd->nx + 1u;
+    v.uy = (uint32_t)gd->ny + 1u;
+    v.uz = (uint32_t)gd->nz + 1u;
     const DevInstance* d_inst = (const DevInstance*)tables;
     const DevModel* d_models = (const DevModel*)(tables + kNaInstBytes);
     // runs of equal ops, applied in array order (same result as one by one)

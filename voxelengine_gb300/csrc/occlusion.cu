@@ -123,7 +123,7 @@ __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView&
     const TraceConstsP& c = S.c;
     const int R = c.R;
     const unsigned lt_mask = (1u << lane) - 1u;
-    const unsigned ux = (unsigned)g.nx + 1u, uy = (unsigned)g.ny + 1u, uz = (unsigned)g.nz + 1u;
+    const unsigned ux = g.ux, uy = g.uy, uz = g.uz;
 
     // ---------------------------------------------------------- A
     const int p = lane % TP;

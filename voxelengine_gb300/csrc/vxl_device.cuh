@@ -28,6 +28,7 @@ struct GridView {
     uint32_t bxy;  // bricks per z slice
     int tx;        // tiles along x
     uint32_t txy;  // tiles per z slice
+    uint32_t ux, uy, uz;  // nx + 1, ny + 1, nz + 1: the DDA's inclusive bounds (Light.frag:53-55)
 };
 
 inline GridView view_of(const vxl_grid* g) {
@@ -41,6 +42,9 @@ inline GridView view_of(const vxl_grid* g) {
     v.bxy = (uint32_t)g->bx * (uint32_t)g->by;
     v.tx = g->tx;
     v.txy = (uint32_t)g->tx * (uint32_t)g->ty;
+    v.ux = (uint32_t)g->nx + 1u;
+    v.uy = (uint32_t)g->ny + 1u;
+    v.uz = (uint32_t)g->nz + 1u;
     return v;
 }
 
@@ -333,8 +337,7 @@ __device__ __forceinline__ bool dda_leap(DState& s) {
 template <bool LEAP = false>
 __device__ __forceinline__ int dda_run(const GridView& g, DState& s, Hit& r, int budget) {
     for (int it = 0; it < budget; it++) {
-        if ((unsigned)s.cx > (unsigned)g.nx + 1u || (unsigned)s.cy > (unsigned)g.ny + 1u ||
-            (unsigned)s.cz > (unsigned)g.nz + 1u) {
+        if ((unsigned)s.cx > g.ux || (unsigned)s.cy > g.uy || (unsigned)s.cz > g.uz) {
             r = Hit{s.cx, s.cy, s.cz, s.tot, s.n, VXL_RF_EXIT_BOUNDS};
             return VXL_RF_EXIT_BOUNDS;
         }
