@@ -214,7 +214,7 @@ __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView&
                     if (meta & kMetaLit) {
                         const Hit h = dda_literal(g, mk(sl.a0, sl.a1, sl.a2), mk(sl.b0, sl.b1, sl.b2), maxt);
                         const int pp = (meta >> 4) & 31;
-                        if (RECORDS || (h.flags & VXL_RF_HIT)) res_t[k * TP + pp] = h.t;
+                        res_t[k * TP + pp] = h.t;
                         if (h.flags & VXL_RF_HIT) atomicOr(&res_hit[k], 1u << pp);
                         if (RECORDS) {
                             int64_t gp;
@@ -250,9 +250,7 @@ __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView&
             const int f = dda_run<LEAP>(g, s, h, KSTEP);
             if (f) {
                 const int k = (meta >> 9) & 31, pp = (meta >> 4) & 31;
-                // the fold reads t of hits only: a miss's t (the bounds exit's
-                // totalt) is kept for the records alone
-                if (RECORDS || (f & VXL_RF_HIT)) res_t[k * TP + pp] = h.t;
+                res_t[k * TP + pp] = h.t;
                 if (f & VXL_RF_HIT) atomicOr(&res_hit[k], 1u << pp);
                 if (RECORDS) {
                     int64_t gp;
