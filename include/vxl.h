@@ -275,7 +275,9 @@ vxl_status vxl_light_point(vxl_ctx* ctx, const vxl_grid* grid, const float* d_wp
  * when |light.pos - wpos| <= range (the pass's discard test); then the same
  * jittered shadow ray vxl_light_point traces for that light. Out (device
  * uint64 per pixel): bit l of d_lit = in range and unshadowed; bit l of
- * d_in_range (optional) = in range. Host light table. */
+ * d_in_range (optional) = in range. Host light table. Uses a context
+ * workspace of 16 bytes per pixel plus 256 KB (the light grid and the list
+ * of pairs in range). */
 typedef struct vxl_light {
     float pos[3];      /* world units */
     float range;

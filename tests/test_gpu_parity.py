@@ -256,3 +256,76 @@ def test_light_points_fused_matches_per_light(vxl, ctx, g64):
     assert (want_in != 0).mean() > 0.5 and (want_in != want_lit).any()
     with pytest.raises(vxl.VxlError):
         vxl.light_points(ctx, G, dev(wpos), dev(nrm), dev(noise), n, lights + lights[:1], lit)
+
+
+def test_light_points_warp_culling_is_exact(vxl, ctx, g64):
+    """Positions laid out like an image (each warp's 32 pixels close together)
+    so that warps skip the lights whose sphere misses their box; pixels placed
+    at exactly a light's range, a warp of one repeated boundary position, NaN
+    and infinite positions: masks equal the oracle's per-light pass."""
+    import torch
+
+    G = grid_from_r8(vxl, ctx, g64)
+    rng = np.random.default_rng(23)
+    side = 96
+    n = side * side
+    u, v = np.meshgrid(np.arange(side), np.arange(side))
+    wpos = np.stack([0.2 + u * 0.063, 1.5 + 0.8 * np.sin(u * 0.07) * np.cos(v * 0.05), 0.2 + v * 0.063],
+                    -1).reshape(n, 3).astype(np.float32)
+    axes = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1]], np.float32)
+    nrm = axes[rng.integers(0, 6, n)]
+    noise = rng.random((n, 4)).astype(np.float32)
+    lights = [(rng.uniform(0.3, 6.0, 3).astype(np.float32), float(rng.uniform(0.3, 1.2)), bool(l % 3 == 2))
+              for l in range(64)]
+    # pixels at exactly a light's range along an axis, and a whole warp at one such point
+    for j in range(40):
+        lp, r, _ = lights[j]
+        wpos[j * 37 + 5] = lp + np.float32(r) * axes[j % 6]
+    lp, r, _ = lights[3]
+    wpos[32 * 100:32 * 101] = lp + np.float32(r) * axes[2]
+    wpos[32 * 50 + 7] = np.nan
+    wpos[32 * 60 + 3] = [np.inf, 1.0, 1.0]
+    wpos[32 * 61 + 9] = [-np.inf, np.inf, 2.0]
+    lit = torch.full((n,), -1, dtype=torch.int64, device="cuda")
+    inr = torch.full((n,), -1, dtype=torch.int64, device="cuda")
+    vxl.light_points(ctx, G, dev(wpos), dev(nrm), dev(noise), n, lights, lit, inr)
+    torch.cuda.synchronize()
+    want_lit = np.zeros(n, np.uint64)
+    want_in = np.zeros(n, np.uint64)
+    for l, (lp, r, spot) in enumerate(lights):
+        sh, _ = oracle.light_point(g64, wpos, nrm, noise, lp, r, spot=spot, init=np.full(n, -7.0, np.float32))
+        b = np.uint64(1) << np.uint64(l)
+        want_in |= np.where(sh != -7.0, b, np.uint64(0))
+        want_lit |= np.where(sh == 1.0, b, np.uint64(0))
+    assert np.array_equal(inr.cpu().numpy().view(np.uint64), want_in)
+    assert np.array_equal(lit.cpu().numpy().view(np.uint64), want_lit)
+    # the layout lets warps skip most lights: few pairs are in range
+    bits = sum(bin(int(x)).count("1") for x in want_in)
+    assert 0 < bits < n * 64 * 0.2
+
+
+def test_light_points_pair_list_overflow_is_exact(vxl, ctx, g64):
+    """Every (pixel, light) pair in range: far more pairs than the list holds
+    (two per pixel), so most are traced in the first pass; masks equal the
+    oracle's per-light pass."""
+    import torch
+
+    G = grid_from_r8(vxl, ctx, g64)
+    rng = np.random.default_rng(29)
+    n = 20000
+    axes = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1]], np.float32)
+    wpos = rng.uniform(0.2, 6.2, (n, 3)).astype(np.float32)
+    nrm = axes[rng.integers(0, 6, n)]
+    noise = rng.random((n, 4)).astype(np.float32)
+    lights = [(rng.uniform(0.5, 6.0, 3).astype(np.float32), 100.0, bool(l % 3 == 2)) for l in range(64)]
+    lit = torch.full((n,), -1, dtype=torch.int64, device="cuda")
+    inr = torch.full((n,), -1, dtype=torch.int64, device="cuda")
+    vxl.light_points(ctx, G, dev(wpos), dev(nrm), dev(noise), n, lights, lit, inr)
+    torch.cuda.synchronize()
+    want_lit = np.zeros(n, np.uint64)
+    for l, (lp, r, spot) in enumerate(lights):
+        sh, _ = oracle.light_point(g64, wpos, nrm, noise, lp, r, spot=spot, init=np.full(n, -7.0, np.float32))
+        want_lit |= np.where(sh == 1.0, np.uint64(1) << np.uint64(l), np.uint64(0))
+    assert np.array_equal(inr.cpu().numpy().view(np.uint64), np.full(n, np.uint64(2**64 - 1)))
+    assert np.array_equal(lit.cpu().numpy().view(np.uint64), want_lit)
+    assert (want_lit != 0).any() and (want_lit != np.uint64(2**64 - 1)).any()

@@ -216,38 +216,162 @@ struct LightDev {
     float range;
     int spot;
 };
-__global__ void k_light_points(GridView g, const float* __restrict__ wpos, const float* __restrict__ nrm,
-                               const float4* __restrict__ noise, int64_t npix, const LightDev* __restrict__ lights,
-                               unsigned long long* __restrict__ lit, unsigned long long* __restrict__ in_range) {
-    const int l = blockIdx.y;
-    const LightDev Lt = lights[l];
-    const unsigned long long bit = 1ull << l;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npix;
-         i += (int64_t)gridDim.x * blockDim.x) {
+struct LightTable {
+    LightDev l[64];
+    int n;
+};
+
+// The shadow ray of one (pixel, light) pair in range, as vxl_light_point traces
+// it (LightPoint.frag:105-129, LightSpot.frag:93-117): true when unshadowed.
+__device__ __forceinline__ bool light_pair_lit(const GridView& g, f3 worldPos, f3 normal, float4 nz, const LightDev& Lt,
+                                               f3 lightDir, float lightDistance) {
+    f3 wd;
+    float hitDist;
+    if (Lt.spot) {
+        wd = mul(normalize(lightDir), 10.0f);
+        hitDist = lightDistance * 10.0f;
+    } else {
+        wd = lightDir;
+        hitDist = lightDistance * 10.5f;
+    }
+    f3 wcp = mul(worldPos, 10.0f);
+    f3 randomVec = mul(cosine_sample(nz.x, nz.y), 0.1f);
+    randomVec.z *= glsl_sign(nz.z - 0.5f);
+    wd = normalize(mix(wd, randomVec, 0.5f));
+    wcp = add(wcp, mul(wd, nz.w * 1.0f));
+    wcp = add(wcp, mul(randomVec, 2.5f));
+    const Hit h = march(g, add(wcp, mul(normal, 0.5f)), wd, hitDist, Lt.spot ? 2.5f : 0.5f);
+    return !(h.t < hitDist);
+}
+
+// Light grid of the fused lights: kLightCells^3 cells over the box that holds
+// every light's sphere; each cell keeps the mask of lights whose sphere, grown
+// by a margin, touches the cell grown by a margin, so a pixel needs the exact
+// range test for its cell's lights only (a pixel outside the box is in range
+// of none). The margins cover the fp32 rounding of the cell index and of the
+// box distance.
+constexpr int kLightCells = 32;
+struct LightGrid {
+    f3 lo;         // box corner
+    float cell;    // cell edge
+    float inv;     // 1 / cell
+    float slack;   // absolute margin: a few ulps of the largest light coordinate
+    int on;        // 0: every pixel tests every light
+};
+
+__global__ void k_light_grid(const __grid_constant__ LightTable T, LightGrid LG, unsigned long long* __restrict__ masks) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= kLightCells * kLightCells * kLightCells) return;
+    const int cx = c % kLightCells, cy = (c / kLightCells) % kLightCells, cz = c / (kLightCells * kLightCells);
+    const float m = LG.cell * 0.01f + LG.slack;
+    const f3 a = mk(LG.lo.x + (float)cx * LG.cell - m, LG.lo.y + (float)cy * LG.cell - m,
+                    LG.lo.z + (float)cz * LG.cell - m);
+    const f3 b = mk(a.x + LG.cell + 2.0f * m, a.y + LG.cell + 2.0f * m, a.z + LG.cell + 2.0f * m);
+    unsigned long long mask = 0ull;
+    for (int l = 0; l < T.n; l++) {
+        const LightDev& Lt = T.l[l];
+        const float dx = fmaxf(fmaxf(a.x - Lt.pos.x, Lt.pos.x - b.x), 0.0f);
+        const float dy = fmaxf(fmaxf(a.y - Lt.pos.y, Lt.pos.y - b.y), 0.0f);
+        const float dz = fmaxf(fmaxf(a.z - Lt.pos.z, Lt.pos.z - b.z), 0.0f);
+        const float r = fabsf(Lt.range) * 1.0001f + 1e-4f;
+        if (!(dx * dx + dy * dy + dz * dz > r * r)) mask |= 1ull << l;
+    }
+    masks[c] = mask;
+}
+
+// Pass 1 of the fused lights: one thread per pixel. The pixel's candidate
+// lights come from the light grid (all lights for a NaN position or without a
+// grid); the exact per-pixel range test of each candidate sets the in-range
+// mask. Pairs in range are appended to a list (one atomic per warp) for pass 2,
+// which traces them with full warps; pairs past the list's capacity are traced
+// here.
+__global__ void __launch_bounds__(256) k_light_points(GridView g, const float* __restrict__ wpos,
+                                                      const float* __restrict__ nrm, const float4* __restrict__ noise,
+                                                      int64_t npix, const __grid_constant__ LightTable T, LightGrid LG,
+                                                      const unsigned long long* __restrict__ masks,
+                                                      unsigned long long* __restrict__ lit,
+                                                      unsigned long long* __restrict__ in_range,
+                                                      unsigned long long* __restrict__ pairs,
+                                                      unsigned long long* __restrict__ npairs, uint64_t cap) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned long long all = T.n >= 64 ? ~0ull : ((1ull << T.n) - 1ull);
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < npix; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = base + threadIdx.x;
+        const bool valid = i < npix;
+        const f3 worldPos = valid ? ld3(wpos + 3 * i) : mk(0.0f, 0.0f, 0.0f);
+        unsigned long long cand = 0ull;
+        if (valid) {
+            cand = all;
+            const bool nan_pos = worldPos.x != worldPos.x || worldPos.y != worldPos.y || worldPos.z != worldPos.z;
+            if (LG.on && !nan_pos) {
+                const float fx = floorf((worldPos.x - LG.lo.x) * LG.inv), fy = floorf((worldPos.y - LG.lo.y) * LG.inv),
+                            fz = floorf((worldPos.z - LG.lo.z) * LG.inv);
+                const float top = (float)kLightCells;
+                if (fx >= 0.0f && fy >= 0.0f && fz >= 0.0f && fx < top && fy < top && fz < top)
+                    cand = masks[((int)fz * kLightCells + (int)fy) * kLightCells + (int)fx];
+                else
+                    cand = 0ull;  // outside every light's sphere
+            }
+        }
+        unsigned long long inr = 0ull;
+        for (unsigned long long c = cand; c; c &= c - 1ull) {
+            const int l = __ffsll((long long)c) - 1;
+            const LightDev& Lt = T.l[l];
+            const f3 lightDir = sub(Lt.pos, worldPos);
+            const float lightDistance = sqrtf(dot(lightDir, lightDir));
+            if (!(lightDistance > Lt.range)) inr |= 1ull << l;  // else the light's pass discards this pixel
+        }
+        // one list slot per pair in range: warp prefix sum, one atomic per warp
+        const int cnt = __popcll(inr);
+        int pre = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(full, pre, o);
+            if (lane >= o) pre += y;
+        }
+        const int total = __shfl_sync(full, pre, 31);
+        unsigned long long at0 = 0ull;
+        if (lane == 0 && total > 0) at0 = atomicAdd(npairs, (unsigned long long)total);
+        at0 = __shfl_sync(full, at0, 0) + (unsigned long long)(pre - cnt);
+        unsigned long long litm = 0ull;
+        for (unsigned long long c = inr; c; c &= c - 1ull, at0++) {
+            const int l = __ffsll((long long)c) - 1;
+            if (at0 < cap) {
+                pairs[at0] = ((unsigned long long)i << 6) | (unsigned long long)l;
+            } else {
+                const LightDev& Lt = T.l[l];
+                const f3 lightDir = sub(Lt.pos, worldPos);
+                const float lightDistance = sqrtf(dot(lightDir, lightDir));
+                if (light_pair_lit(g, worldPos, ld3(nrm + 3 * i), noise[i], Lt, lightDir, lightDistance))
+                    litm |= 1ull << l;
+            }
+        }
+        if (valid) {
+            lit[i] = litm;
+            if (in_range) in_range[i] = inr;
+        }
+    }
+}
+
+// Pass 2: the listed (pixel, light) pairs, one per thread.
+__global__ void __launch_bounds__(256) k_light_pairs(GridView g, const float* __restrict__ wpos,
+                                                     const float* __restrict__ nrm, const float4* __restrict__ noise,
+                                                     const __grid_constant__ LightTable T,
+                                                     const unsigned long long* __restrict__ pairs,
+                                                     const unsigned long long* __restrict__ npairs, uint64_t cap,
+                                                     unsigned long long* __restrict__ lit) {
+    const unsigned long long n = *npairs < cap ? *npairs : cap;
+    for (unsigned long long e = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; e < n;
+         e += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned long long pr = pairs[e];
+        const int64_t i = (int64_t)(pr >> 6);
+        const int l = (int)(pr & 63ull);
+        const LightDev& Lt = T.l[l];
         const f3 worldPos = ld3(wpos + 3 * i);
         const f3 lightDir = sub(Lt.pos, worldPos);
         const float lightDistance = sqrtf(dot(lightDir, lightDir));
-        if (lightDistance > Lt.range) continue;  // the light's pass discards this pixel
-        const float4 nz = noise[i];
-        const f3 normal = ld3(nrm + 3 * i);
-        f3 wd;
-        float hitDist;
-        if (Lt.spot) {
-            wd = mul(normalize(lightDir), 10.0f);
-            hitDist = lightDistance * 10.0f;
-        } else {
-            wd = lightDir;
-            hitDist = lightDistance * 10.5f;
-        }
-        f3 wcp = mul(worldPos, 10.0f);
-        f3 randomVec = mul(cosine_sample(nz.x, nz.y), 0.1f);
-        randomVec.z *= glsl_sign(nz.z - 0.5f);
-        wd = normalize(mix(wd, randomVec, 0.5f));
-        wcp = add(wcp, mul(wd, nz.w * 1.0f));
-        wcp = add(wcp, mul(randomVec, 2.5f));
-        const Hit h = march(g, add(wcp, mul(normal, 0.5f)), wd, hitDist, Lt.spot ? 2.5f : 0.5f);
-        if (in_range) atomicOr(in_range + i, bit);
-        if (!(h.t < hitDist)) atomicOr(lit + i, bit);
+        if (light_pair_lit(g, worldPos, ld3(nrm + 3 * i), noise[i], Lt, lightDir, lightDistance))
+            atomicOr(lit + i, 1ull << l);
     }
 }
 
@@ -354,26 +478,61 @@ vxl_status launch_light_point(vxl_ctx* ctx, const vxl_grid* g, const float* wpos
 vxl_status launch_light_points(vxl_ctx* ctx, const vxl_grid* g, const float* wpos, const float* nrm,
                                const float* noise, int64_t npix, const vxl_light* lights, int nlights,
                                unsigned long long* lit, unsigned long long* in_range, cudaStream_t s) {
-    VXL_TRY_CUDA(cudaMemsetAsync(lit, 0, sizeof(unsigned long long) * (size_t)npix, s));
-    if (in_range) VXL_TRY_CUDA(cudaMemsetAsync(in_range, 0, sizeof(unsigned long long) * (size_t)npix, s));
-    if (npix <= 0 || nlights <= 0) return VXL_OK;
-    LightDev h[64];
-    for (int l = 0; l < nlights; l++) {
-        h[l].pos = mk(lights[l].pos[0], lights[l].pos[1], lights[l].pos[2]);
-        h[l].range = lights[l].range;
-        h[l].spot = lights[l].spot ? 1 : 0;
+    if (npix <= 0) return VXL_OK;
+    LightTable T;
+    T.n = nlights > 0 ? nlights : 0;
+    for (int l = 0; l < T.n; l++) {
+        T.l[l].pos = mk(lights[l].pos[0], lights[l].pos[1], lights[l].pos[2]);
+        T.l[l].range = lights[l].range;
+        T.l[l].spot = lights[l].spot ? 1 : 0;
     }
-    void* p;
-    VXL_TRY(ctx_scratch(ctx, sizeof(LightDev) * 64, &p));
-    VXL_TRY_CUDA(cudaMemcpyAsync(p, h, sizeof(LightDev) * (size_t)nlights, cudaMemcpyHostToDevice, s));
+    // light grid over the box of every light's sphere (off when a light's
+    // position or range is not finite)
+    constexpr int kCells = kLightCells * kLightCells * kLightCells;
+    LightGrid LG{mk(0.0f, 0.0f, 0.0f), 1.0f, 1.0f, 0.0f, T.n > 0 ? 1 : 0};
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY}, maxabs = 0.0f;
+    for (int l = 0; l < T.n; l++) {
+        const float r = std::fabs(lights[l].range);
+        for (int a = 0; a < 3; a++) {
+            if (!std::isfinite(lights[l].pos[a]) || !std::isfinite(r)) LG.on = 0;
+            lo[a] = std::min(lo[a], lights[l].pos[a] - r);
+            hi[a] = std::max(hi[a], lights[l].pos[a] + r);
+            maxabs = std::max(maxabs, std::fabs(lights[l].pos[a]) + r);
+        }
+    }
+    if (LG.on) {
+        LG.slack = 1e-4f + maxabs * 4e-7f;
+        float ext = 0.0f;
+        for (int a = 0; a < 3; a++) ext = std::max(ext, hi[a] - lo[a]);
+        ext = std::max(ext + 2.0f * LG.slack, 1e-3f) * 1.002f;
+        LG.cell = ext / (float)kLightCells;
+        LG.inv = 1.0f / LG.cell;
+        LG.lo = mk(lo[0] - LG.slack - 0.001f * ext, lo[1] - LG.slack - 0.001f * ext, lo[2] - LG.slack - 0.001f * ext);
+        if (!std::isfinite(LG.cell) || !std::isfinite(LG.inv) || !std::isfinite(maxabs)) LG.on = 0;
+    }
+    // pair list: two pairs per pixel (frames with more trace the rest in pass 1)
+    const uint64_t cap = (uint64_t)std::max<int64_t>(2 * npix, 1 << 16);
+    VXL_TRY(ctx_grow(&ctx->d_lpairs, &ctx->lpairs_bytes, (size_t)(cap + 1 + kCells) * sizeof(unsigned long long)));
+    unsigned long long* npairs = (unsigned long long*)ctx->d_lpairs;
+    unsigned long long* masks = npairs + 1;
+    unsigned long long* pairs = masks + kCells;
+    VXL_TRY_CUDA(cudaMemsetAsync(npairs, 0, sizeof(unsigned long long), s));
     GridView v = view_of(g);
-    int64_t bx = (npix + 127) / 128;
-    const int64_t cap = (int64_t)ctx->sm_count * 16 * 4 / nlights + 1;
-    if (bx > cap) bx = cap;
-    dim3 grid((unsigned)bx, (unsigned)nlights);
-    k_light_points<<<grid, 128, 0, s>>>(v, wpos, nrm, (const float4*)noise, npix, (const LightDev*)p, lit, in_range);
+    if (LG.on) {
+        k_light_grid<<<(kCells + 255) / 256, 256, 0, s>>>(T, LG, masks);
+        ctx->launches++;
+    }
+    const int64_t bx = std::min<int64_t>((npix + 255) / 256, (int64_t)ctx->sm_count * 8);
+    k_light_points<<<(unsigned)bx, 256, 0, s>>>(v, wpos, nrm, (const float4*)noise, npix, T, LG, masks, lit, in_range,
+                                                pairs, npairs, cap);
     ctx->launches++;
     VXL_TRY_CUDA(cudaGetLastError());
+    if (T.n > 0) {
+        k_light_pairs<<<(unsigned)ctx->sm_count * 8, 256, 0, s>>>(v, wpos, nrm, (const float4*)noise, T, pairs, npairs,
+                                                                  cap, lit);
+        ctx->launches++;
+        VXL_TRY_CUDA(cudaGetLastError());
+    }
     return VXL_OK;
 }
 

@@ -226,6 +226,7 @@ vxl_status vxl_ctx_destroy(vxl_ctx* ctx) {
     if (ctx->h_pin) cudaFreeHost(ctx->h_pin);
     if (ctx->d_taa) cudaFree(ctx->d_taa);
     if (ctx->d_fd) cudaFree(ctx->d_fd);
+    if (ctx->d_lpairs) cudaFree(ctx->d_lpairs);
     delete ctx;
     return VXL_OK;
 }

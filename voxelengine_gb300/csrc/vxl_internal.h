@@ -42,6 +42,9 @@ struct vxl_ctx {
     // positions and sky-masked normals rebuilt from a depth G-buffer
     void* d_fd;
     size_t fd_bytes;
+    // fused lights: count and list of (pixel, light) pairs in range
+    void* d_lpairs;
+    size_t lpairs_bytes;
 };
 constexpr uint32_t kCounterRing = 4096;
 
