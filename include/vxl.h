@@ -294,7 +294,8 @@ vxl_status vxl_light_points(vxl_ctx* ctx, const vxl_grid* grid, const float* d_w
  * clamp to edge, texel centres at (i + 0.5) / size) at UV = ((px + .5) / W,
  * (py + .5) / H); sin/cos are the library's own. Out: float[npix][4]
  * (accumulated rgb, variance), the next frame's last_light. The 4-channel
- * images must be 16-byte aligned and motion 8-byte aligned. */
+ * images must be 16-byte aligned and motion 8-byte aligned. Uses a context
+ * workspace of 64 bytes per pixel (the texels the taps read, regrouped). */
 typedef struct vxl_taa_frame {
     const float* light;       /* [4] this frame's lighting */
     const float* last_light;  /* [4] the previous output (rgb, variance in a) */

@@ -35,8 +35,9 @@ __device__ __forceinline__ float gmax(float x, float y) { return (x < y) ? y : x
 __device__ __forceinline__ float gmin(float x, float y) { return (y < x) ? y : x; }
 __device__ __forceinline__ float clampg(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
 
-template <int C>
-__device__ __forceinline__ void tex(const float* __restrict__ p, int W, int H, float u, float v, float* out) {
+// texture() of a 4-channel image with the pass's sampler (16-byte texels: one
+// vector load each)
+__device__ __forceinline__ void tex4(const float* __restrict__ p, int W, int H, float u, float v, float* out) {
     const float x = u * (float)W - 0.5f, y = v * (float)H - 0.5f;
     const float fx = floorf(x), fy = floorf(y);
     const float ax = x - fx, ay = y - fy;
@@ -46,45 +47,15 @@ __device__ __forceinline__ void tex(const float* __restrict__ p, int W, int H, f
     y0 = y0 < 0 ? 0 : (y0 > H - 1 ? H - 1 : y0);
     y1 = y1 < 0 ? 0 : (y1 > H - 1 ? H - 1 : y1);
     const float bx = 1.0f - ax, by = 1.0f - ay;
-    const size_t i00 = ((size_t)y0 * W + x0) * C, i10 = ((size_t)y0 * W + x1) * C;
-    const size_t i01 = ((size_t)y1 * W + x0) * C, i11 = ((size_t)y1 * W + x1) * C;
-    float t00[C], t10[C], t01[C], t11[C];
-    if (C == 4) {  // 16-byte texels: one vector load each
-        const float4 a = __ldg(reinterpret_cast<const float4*>(p + i00)), b = __ldg(reinterpret_cast<const float4*>(p + i10));
-        const float4 c = __ldg(reinterpret_cast<const float4*>(p + i01)), d = __ldg(reinterpret_cast<const float4*>(p + i11));
-        const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
-        const float cv[4] = {c.x, c.y, c.z, c.w}, dv[4] = {d.x, d.y, d.z, d.w};
+    const float4* q = reinterpret_cast<const float4*>(p);
+    const float4 a = __ldg(q + ((size_t)y0 * W + x0)), b = __ldg(q + ((size_t)y0 * W + x1));
+    const float4 c = __ldg(q + ((size_t)y1 * W + x0)), d = __ldg(q + ((size_t)y1 * W + x1));
+    const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+    const float cv[4] = {c.x, c.y, c.z, c.w}, dv[4] = {d.x, d.y, d.z, d.w};
 #pragma unroll
-        for (int k = 0; k < C; k++) {
-            t00[k] = av[k];
-            t10[k] = bv[k];
-            t01[k] = cv[k];
-            t11[k] = dv[k];
-        }
-    } else if (C == 2) {
-        const float2 a = __ldg(reinterpret_cast<const float2*>(p + i00)), b = __ldg(reinterpret_cast<const float2*>(p + i10));
-        const float2 c = __ldg(reinterpret_cast<const float2*>(p + i01)), d = __ldg(reinterpret_cast<const float2*>(p + i11));
-        const float av[2] = {a.x, a.y}, bv[2] = {b.x, b.y}, cv[2] = {c.x, c.y}, dv[2] = {d.x, d.y};
-#pragma unroll
-        for (int k = 0; k < C; k++) {
-            t00[k] = av[k];
-            t10[k] = bv[k];
-            t01[k] = cv[k];
-            t11[k] = dv[k];
-        }
-    } else {
-#pragma unroll
-        for (int k = 0; k < C; k++) {
-            t00[k] = __ldg(p + i00 + k);
-            t10[k] = __ldg(p + i10 + k);
-            t01[k] = __ldg(p + i01 + k);
-            t11[k] = __ldg(p + i11 + k);
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < C; k++) {
-        const float top = t00[k] * bx + t10[k] * ax;
-        const float bot = t01[k] * bx + t11[k] * ax;
+    for (int k = 0; k < 4; k++) {
+        const float top = av[k] * bx + bv[k] * ax;
+        const float bot = cv[k] * bx + dv[k] * ax;
         out[k] = top * by + bot * ay;
     }
 }
@@ -143,7 +114,7 @@ __device__ __forceinline__ void lerp4(const float4& a, const float4& b, const fl
     }
 }
 
-// The same coordinates, clamping and weights as tex<C>, over the planes.
+// The same coordinates, clamping and weights as tex4, over the planes.
 __device__ __forceinline__ void tap(const float4* __restrict__ rec, int W, int H, float u, float v, Tap* t) {
     const float x = u * (float)W - 0.5f, y = v * (float)H - 0.5f;
     const float fx = floorf(x), fy = floorf(y);
@@ -236,7 +207,7 @@ __global__ void __launch_bounds__(128) k_taa(const TaaIn I, const float4* __rest
         c.de = t.de;
         c.mo[0] = t.mo[0];
         c.mo[1] = t.mo[1];
-        tex<4>(I.light, W, H, c.uvx, c.uvy, cl);
+        tex4(I.light, W, H, c.uvx, c.uvy, cl);
         if (c.de == 1.0f) {
             o[0] = cl[0];
             o[1] = cl[1];
@@ -244,7 +215,7 @@ __global__ void __launch_bounds__(128) k_taa(const TaaIn I, const float4* __rest
             o[3] = cl[3];
         } else {
             const float oux = c.uvx + c.mo[0], ouy = c.uvy + c.mo[1];
-            tex<4>(I.last, W, H, oux, ouy, ll);
+            tex4(I.last, W, H, oux, ouy, ll);
             mode = (clampg(oux, 0.0f, 1.0f) != oux || clampg(ouy, 0.0f, 1.0f) != ouy) ? 1 : 2;
         }
     }
