@@ -207,10 +207,11 @@ __global__ void k_light_point(GridView g, const float* __restrict__ wpos, const 
     }
 }
 
-// Fused point / spot shadows: threads over (pixel, light) with the light as
-// blockIdx.y, so a warp traces one light's rays from 32 neighbouring pixels.
-// The ray of each pair is the one k_light_point traces for that light alone;
-// the results are OR-ed into per-pixel 64-bit masks.
+// Fused point / spot shadows for up to 64 lights (vxl_light_points): a light
+// grid narrows each pixel's candidate lights, pass 1 runs the exact range
+// tests and lists the pairs in range, pass 2 traces each listed pair's ray --
+// the one k_light_point traces for that light alone -- and sets its bit in the
+// pixel's 64-bit mask.
 struct LightDev {
     f3 pos;
     float range;
