@@ -100,6 +100,13 @@ __device__ __forceinline__ f3 gen_dir(const TraceConstsP& c, int k, uint32_t pix
     return normalize(sub(mul(H, 2.0f * vh), V));
 }
 
+// lanes below this one (read at each use rather than kept in a register)
+__device__ __forceinline__ unsigned lanes_below() {
+    unsigned m;
+    asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
 // pixel index of position p of a scene-local tile; false outside the image
 template <int TP>
 __device__ __forceinline__ bool tile_pixel(const SceneDesc& S, int64_t tile, int p, int64_t* gpix) {
@@ -122,7 +129,6 @@ __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView&
     constexpr int LPP = 32 / TP;  // lanes per pixel during generation
     const TraceConstsP& c = S.c;
     const int R = c.R;
-    const unsigned lt_mask = (1u << lane) - 1u;
     const unsigned ux = g.ux, uy = g.uy, uz = g.uz;
 
     // ---------------------------------------------------------- A
@@ -189,7 +195,7 @@ __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView&
             store_record(S.rec + gpix * R + k, z);
         }
         const unsigned lv = __ballot_sync(0xffffffffu, is_live);
-        if (is_live) slots[live + __popc(lv & lt_mask)] = sl;
+        if (is_live) slots[live + __popc(lv & lanes_below())] = sl;
         live += __popc(lv);
     }
     __syncwarp();
@@ -205,7 +211,7 @@ __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView&
         const unsigned nm = __ballot_sync(0xffffffffu, need);
         if (nm) {
             if (need) {
-                const int at = base + __popc(nm & lt_mask);
+                const int at = base + __popc(nm & lanes_below());
                 if (at < live) {
                     const PSlot sl = slots[at];
                     meta = (unsigned)sl.c2m >> 16;
@@ -325,8 +331,8 @@ __global__ void __launch_bounds__(128, VXL_POOL_MIN_BLOCKS) k_occl_pool(const Sc
         if (lane == 0) t0 = (int64_t)atomicAdd(counter, (unsigned long long)grab);
         t0 = __shfl_sync(0xffffffffu, t0, 0);
         if (t0 >= S.ntiles) break;
-        for (int64_t t = t0; t < t0 + grab && t < S.ntiles; t++)
-            process_tile<TP, KSTEP, LEAP, RECORDS>(S, g, t, slots, res_t, res_hit, lane);
+        for (int k = 0; k < grab && t0 + k < S.ntiles; k++)
+            process_tile<TP, KSTEP, LEAP, RECORDS>(S, g, t0 + k, slots, res_t, res_hit, lane);
     }
 }
 
