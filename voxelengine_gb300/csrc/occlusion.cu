@@ -351,7 +351,8 @@ __global__ void __launch_bounds__(128, VXL_POOL_MIN_BLOCKS) k_occl_batch(const S
         if (lane == 0) t0 = (int64_t)atomicAdd(counter, (unsigned long long)grab);
         t0 = __shfl_sync(0xffffffffu, t0, 0);
         if (t0 >= total_tiles) break;
-        for (int64_t t = t0; t < t0 + grab && t < total_tiles; t++) {
+        for (int k = 0; k < grab && t0 + k < total_tiles; k++) {
+            const int64_t t = t0 + k;
             int lo = 0, hi = nscenes - 1;  // last scene with tile_begin <= t
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
