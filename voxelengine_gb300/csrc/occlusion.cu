@@ -123,7 +123,9 @@ __device__ __forceinline__ bool tile_pixel(const SceneDesc& S, int64_t tile, int
 }
 
 // Phases A-C for one tile of one scene.
-template <int TP, int KSTEP, bool LEAP, bool RECORDS>
+// HIT_T: write a ray's t for hits only (the fold reads no other); the batched
+// kernel keeps writing every t, which its register allocation prefers
+template <int TP, int KSTEP, bool LEAP, bool RECORDS, bool HIT_T = false>
 __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView& g, int64_t tile, PSlot* slots,
                                              float* res_t, uint32_t* res_hit, int lane) {
     constexpr int LPP = 32 / TP;  // lanes per pixel during generation
@@ -202,12 +204,12 @@ __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView&
 
     // ---------------------------------------------------------- B
     int base = 0;
-    int my = -1;
+    bool busy = false;  // the lane holds a ray
     bool retired = false;
     DState s;
     int meta = 0;
     for (;;) {
-        const bool need = my < 0 && !retired;
+        const bool need = !busy && !retired;
         const unsigned nm = __ballot_sync(0xffffffffu, need);
         if (nm) {
             if (need) {
@@ -220,7 +222,7 @@ __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView&
                     if (meta & kMetaLit) {
                         const Hit h = dda_literal(g, mk(sl.a0, sl.a1, sl.a2), mk(sl.b0, sl.b1, sl.b2), maxt);
                         const int pp = (meta >> 4) & 31;
-                        res_t[k * TP + pp] = h.t;
+                        if (!HIT_T || (h.flags & VXL_RF_HIT)) res_t[k * TP + pp] = h.t;
                         if (h.flags & VXL_RF_HIT) atomicOr(&res_hit[k], 1u << pp);
                         if (RECORDS) {
                             int64_t gp;
@@ -228,7 +230,7 @@ __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView&
                             store_record(S.rec + gp * R + k, h);
                         }
                     } else {
-                        my = at;
+                        busy = true;
                         s.cx = lo16(sl.c01);
                         s.cy = hi16(sl.c01);
                         s.cz = lo16(sl.c2m);
@@ -250,20 +252,20 @@ __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView&
             }
             base += __popc(nm);
         }
-        if (!__any_sync(0xffffffffu, my >= 0) && base >= live) break;
-        if (my >= 0) {
+        if (!__any_sync(0xffffffffu, busy) && base >= live) break;
+        if (busy) {
             Hit h;
             const int f = dda_run<LEAP>(g, s, h, KSTEP);
             if (f) {
                 const int k = (meta >> 9) & 31, pp = (meta >> 4) & 31;
-                res_t[k * TP + pp] = h.t;
+                if (!HIT_T || (f & VXL_RF_HIT)) res_t[k * TP + pp] = h.t;
                 if (f & VXL_RF_HIT) atomicOr(&res_hit[k], 1u << pp);
                 if (RECORDS) {
                     int64_t gp;
                     tile_pixel<TP>(S, tile, pp, &gp);
                     store_record(S.rec + gp * R + k, h);
                 }
-                my = -1;
+                busy = false;
             }
         }
     }
@@ -332,7 +334,7 @@ __global__ void __launch_bounds__(128, VXL_POOL_MIN_BLOCKS) k_occl_pool(const Sc
         t0 = __shfl_sync(0xffffffffu, t0, 0);
         if (t0 >= S.ntiles) break;
         for (int k = 0; k < grab && t0 + k < S.ntiles; k++)
-            process_tile<TP, KSTEP, LEAP, RECORDS>(S, g, t0 + k, slots, res_t, res_hit, lane);
+            process_tile<TP, KSTEP, LEAP, RECORDS, !RECORDS>(S, g, t0 + k, slots, res_t, res_hit, lane);
     }
 }
 
