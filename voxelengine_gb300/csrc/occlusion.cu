@@ -125,7 +125,7 @@ __device__ __forceinline__ bool tile_pixel(const SceneDesc& S, int64_t tile, int
 // Phases A-C for one tile of one scene.
 // HIT_T: write a ray's t for hits only (the fold reads no other); the batched
 // kernel keeps writing every t, which its register allocation prefers
-template <int TP, int KSTEP, bool LEAP, bool RECORDS, bool HIT_T = false>
+template <int TP, int KSTEP, bool LEAP, bool RECORDS, bool HIT_T = false, bool CACHE = true>
 __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView& g, int64_t tile, PSlot* slots,
                                              float* res_t, uint32_t* res_hit, int lane) {
     constexpr int LPP = 32 / TP;  // lanes per pixel during generation
@@ -255,7 +255,7 @@ __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView&
         if (!__any_sync(0xffffffffu, busy) && base >= live) break;
         if (busy) {
             Hit h;
-            const int f = dda_run<LEAP>(g, s, h, KSTEP);
+            const int f = dda_run<LEAP, CACHE>(g, s, h, KSTEP);
             if (f) {
                 const int k = (meta >> 9) & 31, pp = (meta >> 4) & 31;
                 if (!HIT_T || (f & VXL_RF_HIT)) res_t[k * TP + pp] = h.t;
@@ -318,7 +318,7 @@ __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView&
 #endif
 
 // one scene; its descriptor lives in kernel parameter space
-template <int TP, int KSTEP, bool LEAP, bool RECORDS>
+template <int TP, int KSTEP, bool LEAP, bool RECORDS, bool CACHE = true>
 __global__ void __launch_bounds__(128, VXL_POOL_MIN_BLOCKS) k_occl_pool(const SceneDesc S, unsigned long long* __restrict__ counter,
                                                                         int grab) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -334,13 +334,13 @@ __global__ void __launch_bounds__(128, VXL_POOL_MIN_BLOCKS) k_occl_pool(const Sc
         t0 = __shfl_sync(0xffffffffu, t0, 0);
         if (t0 >= S.ntiles) break;
         for (int k = 0; k < grab && t0 + k < S.ntiles; k++)
-            process_tile<TP, KSTEP, LEAP, RECORDS, !RECORDS>(S, g, t0 + k, slots, res_t, res_hit, lane);
+            process_tile<TP, KSTEP, LEAP, RECORDS, !RECORDS, CACHE>(S, g, t0 + k, slots, res_t, res_hit, lane);
     }
 }
 
 // many scenes, one counter over all their tiles (work stealing across scenes);
 // tiles are numbered scene after scene, table[i].tile_begin ascending
-template <int TP, int KSTEP, bool LEAP>
+template <int TP, int KSTEP, bool LEAP, bool CACHE = true>
 __global__ void __launch_bounds__(128, VXL_POOL_MIN_BLOCKS) k_occl_batch(const SceneDesc* __restrict__ table,
                                                                          int nscenes, int64_t total_tiles,
                                                                          int max_r, unsigned long long* __restrict__ counter,
@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(128, VXL_POOL_MIN_BLOCKS) k_occl_batch(const S
             float* res_t = reinterpret_cast<float*>(wbase + (size_t)TP * R * sizeof(PSlot));
             uint32_t* res_hit = reinterpret_cast<uint32_t*>(wbase + (size_t)TP * R * (sizeof(PSlot) + sizeof(float)));
             const GridView g = S.g;
-            process_tile<TP, KSTEP, LEAP, false>(S, g, t - S.tile_begin, slots, res_t, res_hit, lane);
+            process_tile<TP, KSTEP, LEAP, false, false, CACHE>(S, g, t - S.tile_begin, slots, res_t, res_hit, lane);
         }
     }
 }
@@ -433,11 +433,11 @@ static vxl_status blocks_for_kernel(vxl_ctx* ctx, K kern, size_t smem, int* bloc
     return VXL_OK;
 }
 
-template <int TP, int KSTEP, bool LEAP, bool REC>
+template <int TP, int KSTEP, bool LEAP, bool REC, bool CACHE = true>
 static vxl_status launch_pool_t(vxl_ctx* ctx, const SceneDesc& S, unsigned long long* counter, int grab,
                                 cudaStream_t s) {
     const size_t smem = pool_bytes(TP, S.c.R) * 4;
-    auto kern = k_occl_pool<TP, KSTEP, LEAP, REC>;
+    auto kern = k_occl_pool<TP, KSTEP, LEAP, REC, CACHE>;
     int per_sm = 0;
     VXL_TRY(blocks_for_kernel(ctx, kern, smem, &per_sm));
     int64_t blocks = (int64_t)ctx->sm_count * per_sm;
@@ -449,16 +449,22 @@ static vxl_status launch_pool_t(vxl_ctx* ctx, const SceneDesc& S, unsigned long 
     return VXL_OK;
 }
 
-template <int TP, bool LEAP>
+template <int TP, bool LEAP, bool CACHE>
 static vxl_status launch_pool_k(vxl_ctx* ctx, const SceneDesc& S, unsigned long long* counter, const vxl_tuning& t,
                                 cudaStream_t s) {
     switch (t.kstep) {
-        case 1: return launch_pool_t<TP, 1, LEAP, false>(ctx, S, counter, t.grab, s);
-        case 2: return launch_pool_t<TP, 2, LEAP, false>(ctx, S, counter, t.grab, s);
-        case 4: return launch_pool_t<TP, 4, LEAP, false>(ctx, S, counter, t.grab, s);
-        default: return launch_pool_t<TP, 8, LEAP, false>(ctx, S, counter, t.grab, s);
+        case 1: return launch_pool_t<TP, 1, LEAP, false, CACHE>(ctx, S, counter, t.grab, s);
+        case 2: return launch_pool_t<TP, 2, LEAP, false, CACHE>(ctx, S, counter, t.grab, s);
+        case 4: return launch_pool_t<TP, 4, LEAP, false, CACHE>(ctx, S, counter, t.grab, s);
+        default: return launch_pool_t<TP, 8, LEAP, false, CACHE>(ctx, S, counter, t.grab, s);
     }
 }
+
+// Grids up to this many bytes of brick words stay in L2 while a frame is
+// traced: the traversal then reads the brick word at every step rather than
+// caching it per ray (measured on GB300: +1.8% on a 16 MiB grid, -14% on a
+// 1 GiB one)
+constexpr size_t kStepLoadMaxBytes = (size_t)64 << 20;
 
 bool occl_pool_supported(const vxl_grid* g, const vxl_trace_params* p) {
     int R = p->n_shadow + p->n_ao + p->n_spec;
@@ -479,11 +485,16 @@ vxl_status launch_trace_occlusion_pool(vxl_ctx* ctx, const vxl_grid* g, const vx
         return launch_pool_t<32, 4, false, true>(ctx, S, d_counter, tune.grab, s);
     }
     if (tune.leap == 1) {
-        if (tune.tile_px == 16) return launch_pool_k<16, true>(ctx, S, d_counter, tune, s);
-        return launch_pool_k<32, true>(ctx, S, d_counter, tune, s);
+        if (tune.tile_px == 16) return launch_pool_k<16, true, true>(ctx, S, d_counter, tune, s);
+        return launch_pool_k<32, true, true>(ctx, S, d_counter, tune, s);
     }
-    if (tune.tile_px == 16) return launch_pool_k<16, false>(ctx, S, d_counter, tune, s);
-    return launch_pool_k<32, false>(ctx, S, d_counter, tune, s);
+    const bool cache = g->nwords * sizeof(uint64_t) > kStepLoadMaxBytes;
+    if (tune.tile_px == 16) {
+        if (cache) return launch_pool_k<16, false, true>(ctx, S, d_counter, tune, s);
+        return launch_pool_k<16, false, false>(ctx, S, d_counter, tune, s);
+    }
+    if (cache) return launch_pool_k<32, false, true>(ctx, S, d_counter, tune, s);
+    return launch_pool_k<32, false, false>(ctx, S, d_counter, tune, s);
 }
 
 // ------------------------------------------------------------------ batch
@@ -494,12 +505,13 @@ struct BatchPlan {
     int64_t total_tiles;
     vxl_tuning tune;
     unsigned long long* counter;
+    bool cache;  // some grid of the batch is larger than kStepLoadMaxBytes
 };
 
-template <int TP, int KSTEP>
+template <int TP, int KSTEP, bool CACHE>
 static vxl_status launch_batch_t(vxl_ctx* ctx, const BatchPlan& b, cudaStream_t s) {
     const size_t smem = pool_bytes(TP, b.max_r) * 4;
-    auto kern = k_occl_batch<TP, KSTEP, false>;
+    auto kern = k_occl_batch<TP, KSTEP, false, CACHE>;
     int per_sm = 0;
     VXL_TRY(blocks_for_kernel(ctx, kern, smem, &per_sm));
     int64_t blocks = (int64_t)ctx->sm_count * per_sm;
@@ -511,24 +523,26 @@ static vxl_status launch_batch_t(vxl_ctx* ctx, const BatchPlan& b, cudaStream_t 
     return VXL_OK;
 }
 
-template <int TP>
+template <int TP, bool CACHE>
 static vxl_status launch_batch_k(vxl_ctx* ctx, const BatchPlan& b, cudaStream_t s) {
     switch (b.tune.kstep) {
-        case 1: return launch_batch_t<TP, 1>(ctx, b, s);
-        case 2: return launch_batch_t<TP, 2>(ctx, b, s);
-        case 4: return launch_batch_t<TP, 4>(ctx, b, s);
-        default: return launch_batch_t<TP, 8>(ctx, b, s);
+        case 1: return launch_batch_t<TP, 1, CACHE>(ctx, b, s);
+        case 2: return launch_batch_t<TP, 2, CACHE>(ctx, b, s);
+        case 4: return launch_batch_t<TP, 4, CACHE>(ctx, b, s);
+        default: return launch_batch_t<TP, 8, CACHE>(ctx, b, s);
     }
 }
 
 size_t batch_desc_bytes() { return sizeof(SceneDesc); }
 
 vxl_status batch_build_table(const vxl_batch_item* items, int n, const vxl_tuning& tune, void* h_table, int* max_r,
-                             int64_t* total_tiles, int64_t* total_rays) {
+                             int64_t* total_tiles, int64_t* total_rays, size_t* max_grid_bytes) {
     SceneDesc* t = (SceneDesc*)h_table;
     int64_t tiles = 0, rays = 0;
     int mr = 1;
+    size_t gb = 0;
     for (int i = 0; i < n; i++) {
+        gb = std::max(gb, items[i].grid->nwords * sizeof(uint64_t));
         t[i] = scene_of(items[i].grid, &items[i].gbuf, &items[i].params, &items[i].out, tune);
         t[i].tile_begin = tiles;
         tiles += t[i].ntiles;
@@ -538,15 +552,16 @@ vxl_status batch_build_table(const vxl_batch_item* items, int n, const vxl_tunin
     *max_r = mr;
     *total_tiles = tiles;
     *total_rays = rays;
+    *max_grid_bytes = gb;
     return VXL_OK;
 }
 
 vxl_status launch_batch(vxl_ctx* ctx, void* d_table, int n, int max_r, int64_t total_tiles, const vxl_tuning& tune,
-                        unsigned long long* d_counter, cudaStream_t s) {
-    BatchPlan b{(SceneDesc*)d_table, n, max_r, total_tiles, tune, d_counter};
+                        unsigned long long* d_counter, size_t max_grid_bytes, cudaStream_t s) {
+    BatchPlan b{(SceneDesc*)d_table, n, max_r, total_tiles, tune, d_counter, max_grid_bytes > kStepLoadMaxBytes};
     VXL_TRY_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s));
-    if (tune.tile_px == 16) return launch_batch_k<16>(ctx, b, s);
-    return launch_batch_k<32>(ctx, b, s);
+    if (tune.tile_px == 16) return b.cache ? launch_batch_k<16, true>(ctx, b, s) : launch_batch_k<16, false>(ctx, b, s);
+    return b.cache ? launch_batch_k<32, true>(ctx, b, s) : launch_batch_k<32, false>(ctx, b, s);
 }
 
 }  // namespace vxl

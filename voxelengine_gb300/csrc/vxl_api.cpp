@@ -510,6 +510,7 @@ struct vxl_batch {
     unsigned long long* d_counter;
     int n, max_r;
     int64_t tiles, rays;
+    size_t max_grid_bytes;
     vxl_tuning tune;
     cudaStream_t cap_stream;
     cudaGraph_t graph;
@@ -539,7 +540,7 @@ vxl_status vxl_batch_create(vxl_ctx* ctx, const vxl_batch_item* items, int n, in
     b->n = n;
     b->tune = ctx->tune;
     std::vector<unsigned char> table((size_t)n * batch_desc_bytes());
-    batch_build_table(items, n, b->tune, table.data(), &b->max_r, &b->tiles, &b->rays);
+    batch_build_table(items, n, b->tune, table.data(), &b->max_r, &b->tiles, &b->rays, &b->max_grid_bytes);
     auto cleanup = [b]() {
         if (b->exec) cudaGraphExecDestroy(b->exec);
         if (b->graph) cudaGraphDestroy(b->graph);
@@ -562,7 +563,8 @@ vxl_status vxl_batch_create(vxl_ctx* ctx, const vxl_batch_item* items, int n, in
             cleanup();
             return cuda_fail(e, "batch_create: begin capture");
         }
-        vxl_status st = launch_batch(ctx, b->d_table, n, b->max_r, b->tiles, b->tune, b->d_counter, b->cap_stream);
+        vxl_status st = launch_batch(ctx, b->d_table, n, b->max_r, b->tiles, b->tune, b->d_counter, b->max_grid_bytes,
+                                     b->cap_stream);
         ctx->launches--;  // captured, not run
         e = cudaStreamEndCapture(b->cap_stream, &b->graph);
         if (st != VXL_OK || e != cudaSuccess) {
@@ -588,7 +590,7 @@ vxl_status vxl_batch_run(vxl_batch* b, void* stream) {
         b->ctx->launches++;
         return VXL_OK;
     }
-    return launch_batch(b->ctx, b->d_table, b->n, b->max_r, b->tiles, b->tune, b->d_counter, s);
+    return launch_batch(b->ctx, b->d_table, b->n, b->max_r, b->tiles, b->tune, b->d_counter, b->max_grid_bytes, s);
 }
 
 vxl_status vxl_batch_destroy(vxl_batch* b) {

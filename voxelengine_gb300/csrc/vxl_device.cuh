@@ -334,19 +334,28 @@ __device__ __forceinline__ bool dda_leap(DState& s) {
 // Returns 0 while the ray goes on; otherwise the record flags, r filled in.
 // After a leap (s.leap) a miss may report an approximate cell, t and count;
 // hits are always found by exact stepping.
-template <bool LEAP = false>
+// CACHE: keep the current brick word in registers (one load per brick
+// entered); otherwise read it at every step, which is faster while the grid
+// stays in L2 (fewer live registers) and slower for grids that do not.
+template <bool LEAP = false, bool CACHE = true>
 __device__ __forceinline__ int dda_run(const GridView& g, DState& s, Hit& r, int budget) {
     for (int it = 0; it < budget; it++) {
         if ((unsigned)s.cx > g.ux || (unsigned)s.cy > g.uy || (unsigned)s.cz > g.uz) {
             r = Hit{s.cx, s.cy, s.cz, s.tot, s.n, VXL_RF_EXIT_BOUNDS};
             return VXL_RF_EXIT_BOUNDS;
         }
-        const uint32_t wi = word_index(g, s.cx, s.cy, s.cz);
-        if (wi != s.wcur) {
-            s.wcur = wi;
-            s.word = __ldg(g.words + wi);
+        uint64_t word;
+        if (CACHE) {
+            const uint32_t wi = word_index(g, s.cx, s.cy, s.cz);
+            if (wi != s.wcur) {
+                s.wcur = wi;
+                s.word = __ldg(g.words + wi);
+            }
+            word = s.word;
+        } else {
+            word = __ldg(g.words + word_index(g, s.cx, s.cy, s.cz));
         }
-        if (LEAP && s.leap && s.word == 0ull && dda_leap(s)) {
+        if (LEAP && s.leap && word == 0ull && dda_leap(s)) {
             if (!(s.tot < s.maxt)) {
                 r = Hit{s.cx, s.cy, s.cz, s.tot, s.n, VXL_RF_EXIT_MAXT};
                 return VXL_RF_EXIT_MAXT;
@@ -362,7 +371,7 @@ __device__ __forceinline__ int dda_run(const GridView& g, DState& s, Hit& r, int
             best = (bx ? s.tx : 0.0f) + (by ? s.ty : 0.0f);
             best = best + (bz ? s.tz : 0.0f);
         }
-        if ((s.word >> bit_index(s.cx, s.cy, s.cz)) & 1ull) {
+        if ((word >> bit_index(s.cx, s.cy, s.cz)) & 1ull) {
             const int f = VXL_RF_HIT | (bx ? VXL_RF_SELX : 0) | (by ? VXL_RF_SELY : 0) | (bz ? VXL_RF_SELZ : 0);
             r = Hit{s.cx, s.cy, s.cz, best, s.n + 1, f};
             return f;

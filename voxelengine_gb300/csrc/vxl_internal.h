@@ -136,9 +136,9 @@ unsigned long long* ctx_next_counter(vxl_ctx* ctx);
 // batched occlusion: scene table built on the host, uploaded once, one launch
 size_t batch_desc_bytes();
 vxl_status batch_build_table(const vxl_batch_item* items, int n, const vxl_tuning& tune, void* h_table, int* max_r,
-                             int64_t* total_tiles, int64_t* total_rays);
+                             int64_t* total_tiles, int64_t* total_rays, size_t* max_grid_bytes);
 vxl_status launch_batch(vxl_ctx* ctx, void* d_table, int n, int max_r, int64_t total_tiles, const vxl_tuning& tune,
-                        unsigned long long* d_counter, cudaStream_t s);
+                        unsigned long long* d_counter, size_t max_grid_bytes, cudaStream_t s);
 vxl_status launch_light_ambient(vxl_ctx* ctx, const vxl_grid* g, const float* wcp, const float* nrm,
                                 const float* depth, const float* noise, int64_t npix, float* shadow, float* irr,
                                 vxl_ray_record* rec, cudaStream_t s);
