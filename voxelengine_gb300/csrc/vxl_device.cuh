@@ -337,9 +337,13 @@ __device__ __forceinline__ bool dda_leap(DState& s) {
 // CACHE: keep the current brick word in registers (one load per brick
 // entered); otherwise read it at every step, which is faster while the grid
 // stays in L2 (fewer live registers) and slower for grids that do not.
-template <bool LEAP = false, bool CACHE = true>
+// ONE_COUNT: the step budget and the 256-step cap share one limit, so a step
+// tests one counter (faster in the single-scene pool, slower in the batched
+// one, whose register allocation differs).
+template <bool LEAP = false, bool CACHE = true, bool ONE_COUNT = false>
 __device__ __forceinline__ int dda_run(const GridView& g, DState& s, Hit& r, int budget) {
-    for (int it = 0; it < budget; it++) {
+    const int lim = ONE_COUNT ? min(s.n + budget, 256) : 256;
+    for (int it = 0; ONE_COUNT || it < budget; it++) {
         if ((unsigned)s.cx > g.ux || (unsigned)s.cy > g.uy || (unsigned)s.cz > g.uz) {
             r = Hit{s.cx, s.cy, s.cz, s.tot, s.n, VXL_RF_EXIT_BOUNDS};
             return VXL_RF_EXIT_BOUNDS;
@@ -381,7 +385,8 @@ __device__ __forceinline__ int dda_run(const GridView& g, DState& s, Hit& r, int
         if (by) { s.cy += s.sy; s.ty = s.ty + s.tdy; }
         if (bz) { s.cz += s.sz; s.tz = s.tz + s.tdz; }
         s.tot = best;
-        if (!(++s.n < 256 && best < s.maxt)) {
+        if (!(++s.n < lim && best < s.maxt)) {
+            if (ONE_COUNT && s.n < 256 && best < s.maxt) return 0;  // budget spent; the ray goes on
             // the record reports the last cell tested, not the advanced one
             const int f = s.n >= 256 ? VXL_RF_EXIT_STEPS : VXL_RF_EXIT_MAXT;
             r = Hit{px, py, pz, best, s.n, f};
