@@ -466,6 +466,7 @@ static vxl_status launch_pool_k(vxl_ctx* ctx, const SceneDesc& S, unsigned long 
 // caching it per ray (measured on GB300: +1.8% on a 16 MiB grid, -14% on a
 // 1 GiB one)
 constexpr size_t kStepLoadMaxBytes = (size_t)64 << 20;
+constexpr size_t kPoolSmemPerSm = 228 * 1024;  // shared memory per SM (GB300)
 
 bool occl_pool_supported(const vxl_grid* g, const vxl_trace_params* p) {
     int R = p->n_shadow + p->n_ao + p->n_spec;
@@ -477,6 +478,22 @@ vxl_status launch_trace_occlusion_pool(vxl_ctx* ctx, const vxl_grid* g, const vx
                                        const vxl_trace_params* p, const vxl_outputs* out,
                                        unsigned long long* d_counter, const vxl_tuning& tune, cudaStream_t s,
                                        uint32_t pix_base) {
+    // Many rays per pixel: the 16-pixel pool's shared memory would hold the SM
+    // below the 8 blocks its registers allow, so such frames run 8-pixel tiles
+    // (runs of pixels) in the exact-step kernel.
+    const int R = p->n_shadow + p->n_ao + p->n_spec;
+    if (!out->records && tune.leap != 1 && tune.tile_px == 16 && tune.kstep == 8 &&
+        (pool_bytes(16, R) * 4 + 1024) * VXL_POOL_MIN_BLOCKS > kPoolSmemPerSm) {
+        vxl_tuning t8 = tune;
+        t8.tile_px = 8;
+        t8.tile_w = 8;
+        SceneDesc S8 = scene_of(g, gb, p, out, t8);
+        S8.pix_base = pix_base;
+        VXL_TRY_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s));
+        const bool cache8 = g->nwords * sizeof(uint64_t) > kStepLoadMaxBytes;
+        if (cache8) return launch_pool_t<8, 8, false, false, true>(ctx, S8, d_counter, t8.grab, s);
+        return launch_pool_t<8, 8, false, false, false>(ctx, S8, d_counter, t8.grab, s);
+    }
     SceneDesc S = scene_of(g, gb, p, out, tune);
     S.pix_base = pix_base;
     VXL_TRY_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s));
