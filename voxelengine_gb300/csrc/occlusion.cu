@@ -466,7 +466,6 @@ static vxl_status launch_pool_k(vxl_ctx* ctx, const SceneDesc& S, unsigned long 
 // caching it per ray (measured on GB300: +1.8% on a 16 MiB grid, -14% on a
 // 1 GiB one)
 constexpr size_t kStepLoadMaxBytes = (size_t)64 << 20;
-constexpr size_t kPoolSmemPerSm = 228 * 1024;  // shared memory per SM (GB300)
 
 bool occl_pool_supported(const vxl_grid* g, const vxl_trace_params* p) {
     int R = p->n_shadow + p->n_ao + p->n_spec;
@@ -483,7 +482,7 @@ vxl_status launch_trace_occlusion_pool(vxl_ctx* ctx, const vxl_grid* g, const vx
     // (runs of pixels) in the exact-step kernel.
     const int R = p->n_shadow + p->n_ao + p->n_spec;
     if (!out->records && tune.leap != 1 && tune.tile_px == 16 && tune.kstep == 8 &&
-        (pool_bytes(16, R) * 4 + 1024) * VXL_POOL_MIN_BLOCKS > kPoolSmemPerSm) {
+        (pool_bytes(16, R) * 4 + 1024) * VXL_POOL_MIN_BLOCKS > (size_t)ctx->smem_per_sm) {
         vxl_tuning t8 = tune;
         t8.tile_px = 8;
         t8.tile_w = 8;

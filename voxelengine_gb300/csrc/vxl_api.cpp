@@ -195,6 +195,7 @@ vxl_status vxl_ctx_create(int device, vxl_ctx** out) {
     if (!c) return fail(VXL_ERR_OOM, "ctx_create: host allocation");
     c->device = device;
     e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_counters, kCounterRing * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(c->d_counters, 0, kCounterRing * sizeof(unsigned long long));
     if (e != cudaSuccess) {

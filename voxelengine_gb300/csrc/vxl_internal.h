@@ -11,6 +11,7 @@
 struct vxl_ctx {
     int device;
     int sm_count;
+    int smem_per_sm;  // shared memory per SM, bytes
     uint64_t launches;
     // growable device scratch (voxelizer tables, host-API staging, counters)
     void* d_scratch;
