@@ -50,11 +50,11 @@ const char* vxl_status_string(vxl_status s);
  * host thread, or guard it with a mutex. Replaces the engine's Graphics
  * singleton for this path (Sources/Graphics/Graphics.h:23-32).
  * The calls that use a context workspace (primary visibility, the fused
- * lights, temporal accumulation, the depth-buffer occlusion entry, the
- * voxelizer's tables) reuse it from call to call: on one context, such calls
- * on different streams must not overlap (order them, or use one context per
- * stream). The occlusion and ray-tracing calls keep no shared state between
- * calls and may overlap freely. */
+ * lights, temporal accumulation, the depth-buffer and host-buffer occlusion
+ * entries, the voxelizer's tables) reuse it from call to call: on one context,
+ * such calls on different streams must not overlap (order them, or use one
+ * context per stream). vxl_trace_occlusion and vxl_trace_rays keep no shared
+ * state between calls and may overlap freely. */
 vxl_status vxl_ctx_create(int device, vxl_ctx** out);
 vxl_status vxl_ctx_destroy(vxl_ctx* ctx);
 /* number of kernels this library launched through ctx (diagnostics) */
