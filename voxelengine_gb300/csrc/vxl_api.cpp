@@ -479,13 +479,23 @@ vxl_status vxl_trace_occlusion_host(vxl_ctx* ctx, const vxl_grid* g, const float
     // the chunks start after the work already queued on the caller's stream
     VXL_TRY_CUDA(cudaEventRecord(ctx->pipe_start, s));
     for (int k = 0; k < 2; k++) VXL_TRY_CUDA(cudaStreamWaitEvent(ctx->pipe[k], ctx->pipe_start, 0));
-    const int64_t nchunks = std::min<int64_t>(8, npix / kChunkMin);
-    int64_t chunk = (npix + nchunks - 1) / nchunks;
-    chunk = (chunk + 1023) & ~(int64_t)1023;
-    int c = 0;
-    for (int64_t p0 = 0; p0 < npix; p0 += chunk, c++) {
-        const int64_t n = std::min(chunk, npix - p0);
-        cudaStream_t cs = ctx->pipe[c & 1];
+    // chunk sizes ramp up and down: the first chunk's copy and the last
+    // chunk's read-back are the parts no tracing overlaps
+    static const int kRamp[] = {1, 5, 8, 5, 1};
+    constexpr int kRampN = (int)(sizeof(kRamp) / sizeof(kRamp[0]));
+    int64_t wsum = 0;
+    for (int k = 0; k < kRampN; k++) wsum += kRamp[k];
+    int64_t bounds[kRampN + 1];
+    bounds[0] = 0;
+    for (int k = 0, acc = 0; k < kRampN; k++) {
+        acc += kRamp[k];
+        const int64_t b = k == kRampN - 1 ? npix : (((npix * acc / wsum) + 1023) & ~(int64_t)1023);
+        bounds[k + 1] = std::min(std::max(b, bounds[k]), npix);
+    }
+    for (int ci = 0; ci < kRampN; ci++) {
+        const int64_t p0 = bounds[ci], n = bounds[ci + 1] - bounds[ci];
+        if (n <= 0) continue;
+        cudaStream_t cs = ctx->pipe[ci & 1];
         VXL_TRY_CUDA(cudaMemcpyAsync(d_pos + 3 * p0, h_pos + 3 * p0, (size_t)n * 12, cudaMemcpyHostToDevice, cs));
         VXL_TRY_CUDA(cudaMemcpyAsync(d_nrm + 3 * p0, h_nrm + 3 * p0, (size_t)n * 12, cudaMemcpyHostToDevice, cs));
         if (h_rough)
