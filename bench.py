@@ -68,6 +68,22 @@ def profiled_traffic(workload):
     return None
 
 
+def profiled_pipes(workload):
+    """ALU-pipe and issue-slot utilisation (fractions) of the occlusion kernel
+    from the committed full ncu capture of this workload, or None: the kernel
+    is issue/ALU-bound, which the HBM fraction alone does not show."""
+    p = os.path.join(ROOT, "profiles", "k_occl_pool_%s.md" % workload)
+    if not os.path.exists(p):
+        return None
+    out = {}
+    for line in open(p):
+        for key, name in (("sm__pipe_alu_cycles_active.avg.pct_of_peak_sustained_active", "alu_pipe"),
+                          ("smsp__issue_active.avg.pct_of_peak_sustained_active", "issue_active")):
+            if line.startswith("| `%s` |" % key):
+                out[name] = float(line.split("|")[2].split()[0]) / 100.0
+    return out or None
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -380,6 +396,7 @@ def run_gpu(args, wl):
                      "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one launch, "
                                        "profiles/k_occl_pool_%s.md" % args.workload,
                      "bytes_per_ray": b_ray,
+                     "ncu_pipes": profiled_pipes(args.workload),
                      "note": "algorithmic bytes = ((28 B in + 20 B out) per pixel)/R + 4 B x S_ref per ray; "
                              "per-launch time from CUDA events on the launch stream"},
         "e2e": {"value": e2e, "unit": "Grays/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
