@@ -13,7 +13,9 @@ import oracle
 from tests import prefab_walk, vox_cases
 
 fp = C.POINTER(C.c_float)
-MODS = "/root/reference/Assets/Mods"
+from oracle.ref.build_ref import reference_dir
+
+MODS = os.path.join(reference_dir(), "Assets", "Mods")
 
 
 @pytest.fixture(scope="module")

@@ -78,7 +78,9 @@ def test_read_v_fixture_and_errors(V, tmp_path):
 
 
 def test_read_v_shipped_assets(V):
-    d = "/root/reference/Assets/Mods/default/FarmHouse"
+    from oracle.ref.build_ref import reference_dir
+
+    d = os.path.join(reference_dir(), "Assets", "Mods", "default", "FarmHouse")
     if not os.path.isdir(d):
         pytest.skip("reference assets not present")
     from tests import vox_cases

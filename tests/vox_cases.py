@@ -39,7 +39,11 @@ def read_v(path):
     return np.frombuffer(raw[12:12 + int(sx) * sy * sz], np.uint8).reshape(int(sz), int(sy), int(sx))
 
 
-def farmhouse_models(ref_root="/root/reference", limit=12):
+def farmhouse_models(ref_root=None, limit=12):
+    if ref_root is None:
+        from oracle.ref.build_ref import reference_dir
+
+        ref_root = reference_dir()
     d = os.path.join(ref_root, "Assets", "Mods", "default", "FarmHouse")
     if not os.path.isdir(d):
         return []
