@@ -166,16 +166,17 @@ def test_occlusion_host_entry_matches_device(vxl, ctx):
         assert torch.equal(outs[k].cpu(), hout[k]), k
 
 
-@pytest.mark.parametrize("W,H", [(1280, 720), (1333, 777)])
-def test_occlusion_host_pipeline_matches_one_launch(vxl, ctx, W, H):
+@pytest.mark.parametrize("W,H,n_ao", [(1280, 720, 6), (1333, 777, 6), (1024, 640, 16)])
+def test_occlusion_host_pipeline_matches_one_launch(vxl, ctx, W, H, n_ao):
     """Frames of >= 2^19 pixels go through the chunked copy/compute pipeline
     (pixel chunks on two streams, global pixel index seeding the rays): the
-    outputs equal the one-launch device call bit for bit."""
+    outputs equal the one-launch device call bit for bit. With 18 rays per
+    pixel both run 8-pixel tiles."""
     import torch
 
     G, cam, tgt, pos, nrm, rough = _c1_scene(vxl, ctx, 128, W, H)
     npix = W * H
-    P = vxl.make_params(cam_pos=cam, n_ao=6, ao_len=24.0, n_spec=1, seed=5)
+    P = vxl.make_params(cam_pos=cam, n_ao=n_ao, ao_len=24.0, n_spec=1, seed=5)
     outs = {k: empty(npix, torch.float32) for k in ("shadow", "ao", "ao_vis", "spec", "spec_t")}
     vxl.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, **outs)
     hp, hn, hr = pos.cpu().pin_memory(), nrm.cpu().pin_memory(), rough.cpu().pin_memory()
