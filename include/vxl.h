@@ -220,10 +220,14 @@ vxl_status vxl_trace_occlusion_from_depth(vxl_ctx* ctx, const vxl_grid* grid, co
                                           const vxl_view* view, const vxl_trace_params* params,
                                           const vxl_outputs* out, void* stream);
 
-/* Same, with the G-buffer held in host memory (pinned or pageable): the
- * library copies it in through its context staging buffers, traces, and
- * copies the outputs back to host memory. Synchronous on `stream`. Host
- * outputs may be NULL. */
+/* Same, with the G-buffer held in host memory (pinned or pageable).
+ * When every given buffer is pinned host memory mapped into the device's
+ * address space (cudaHostAlloc / cudaMallocHost / registered memory), the
+ * kernel reads the G-buffer and writes the outputs there directly over the
+ * CPU-GPU link. Otherwise the library copies through its context staging
+ * buffers in a pipeline of pixel chunks, traces, and copies the outputs back.
+ * Both give the same results. Synchronous on `stream`. Host outputs may be
+ * NULL. */
 vxl_status vxl_trace_occlusion_host(vxl_ctx* ctx, const vxl_grid* grid, const float* h_pos, const float* h_nrm,
                                     const float* h_rough, int64_t npix, const vxl_trace_params* params,
                                     float* h_shadow, float* h_ao, float* h_ao_vis, float* h_spec, float* h_spec_t,

@@ -149,7 +149,10 @@ def test_occlusion_leap_matches_exact(vxl, ctx, scene, ao_len, shadow_len):
     assert 0.0 < float(leap["shadow"].mean()) < 1.0
 
 
-def test_occlusion_host_entry_matches_device(vxl, ctx):
+@pytest.mark.parametrize("pinned", [True, False])
+def test_occlusion_host_entry_matches_device(vxl, ctx, pinned):
+    """Host buffers: pinned ones are read and written in place by the kernel,
+    pageable ones go through staged copies; both equal the device call."""
     import torch
 
     G, cam, tgt, pos, nrm, rough = _c1_scene(vxl, ctx, 128, 200, 120)
@@ -157,8 +160,9 @@ def test_occlusion_host_entry_matches_device(vxl, ctx):
     P = vxl.make_params(cam_pos=cam, n_ao=8, ao_len=32.0, n_spec=1, seed=3)
     outs = {k: empty(npix, torch.float32) for k in ("shadow", "ao", "ao_vis", "spec", "spec_t")}
     vxl.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, **outs)
-    hp, hn, hr = pos.cpu().pin_memory(), nrm.cpu().pin_memory(), rough.cpu().pin_memory()
-    hout = {k: torch.zeros(npix, dtype=torch.float32).pin_memory() for k in outs}
+    pin = (lambda t: t.pin_memory()) if pinned else (lambda t: t)
+    hp, hn, hr = pin(pos.cpu()), pin(nrm.cpu()), pin(rough.cpu())
+    hout = {k: pin(torch.zeros(npix, dtype=torch.float32)) for k in outs}
     vxl.trace_occlusion_host(ctx, G, hp, hn, hr, npix, P, h_shadow=hout["shadow"], h_ao=hout["ao"],
                              h_ao_vis=hout["ao_vis"], h_spec=hout["spec"], h_spec_t=hout["spec_t"])
     torch.cuda.synchronize()
@@ -166,12 +170,14 @@ def test_occlusion_host_entry_matches_device(vxl, ctx):
         assert torch.equal(outs[k].cpu(), hout[k]), k
 
 
-@pytest.mark.parametrize("W,H,n_ao", [(1280, 720, 6), (1333, 777, 6), (1024, 640, 16)])
-def test_occlusion_host_pipeline_matches_one_launch(vxl, ctx, W, H, n_ao):
-    """Frames of >= 2^19 pixels go through the chunked copy/compute pipeline
-    (pixel chunks on two streams, global pixel index seeding the rays): the
-    outputs equal the one-launch device call bit for bit. With 18 rays per
-    pixel both run 8-pixel tiles."""
+@pytest.mark.parametrize("W,H,n_ao,pinned", [(1280, 720, 6, False), (1333, 777, 6, False), (1024, 640, 16, False),
+                                              (1333, 777, 6, True)])
+def test_occlusion_host_pipeline_matches_one_launch(vxl, ctx, W, H, n_ao, pinned):
+    """Pageable host buffers of >= 2^19 pixels go through the chunked
+    copy/compute pipeline (pixel chunks on two streams, global pixel index
+    seeding the rays), pinned ones are used in place: the outputs equal the
+    one-launch device call bit for bit. With 18 rays per pixel both run
+    8-pixel tiles."""
     import torch
 
     G, cam, tgt, pos, nrm, rough = _c1_scene(vxl, ctx, 128, W, H)
@@ -179,8 +185,9 @@ def test_occlusion_host_pipeline_matches_one_launch(vxl, ctx, W, H, n_ao):
     P = vxl.make_params(cam_pos=cam, n_ao=n_ao, ao_len=24.0, n_spec=1, seed=5)
     outs = {k: empty(npix, torch.float32) for k in ("shadow", "ao", "ao_vis", "spec", "spec_t")}
     vxl.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, **outs)
-    hp, hn, hr = pos.cpu().pin_memory(), nrm.cpu().pin_memory(), rough.cpu().pin_memory()
-    hout = {k: torch.full((npix,), -3.0, dtype=torch.float32).pin_memory() for k in outs}
+    pin = (lambda t: t.pin_memory()) if pinned else (lambda t: t)
+    hp, hn, hr = pin(pos.cpu()), pin(nrm.cpu()), pin(rough.cpu())
+    hout = {k: pin(torch.full((npix,), -3.0, dtype=torch.float32)) for k in outs}
     vxl.trace_occlusion_host(ctx, G, hp, hn, hr, npix, P, h_shadow=hout["shadow"], h_ao=hout["ao"],
                              h_ao_vis=hout["ao_vis"], h_spec=hout["spec"], h_spec_t=hout["spec_t"])
     torch.cuda.synchronize()

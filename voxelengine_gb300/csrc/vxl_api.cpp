@@ -57,6 +57,23 @@ vxl_status ctx_stage(vxl_ctx* ctx, size_t bytes, void** out) {
     return VXL_OK;
 }
 
+// Device address of host memory the device can reach (pinned, mapped into the
+// unified address space of this context's device); false for anything else,
+// which then goes through explicit copies.
+static bool device_view(const vxl_ctx* ctx, const void* h, void** d) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+        cudaGetLastError();  // clear the error of an unknown pointer
+        return false;
+    }
+    if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr) return false;
+    int mapped = 0;
+    if (cudaDeviceGetAttribute(&mapped, cudaDevAttrCanMapHostMemory, ctx->device) != cudaSuccess || !mapped)
+        return false;
+    *d = a.devicePointer;
+    return true;
+}
+
 unsigned long long* ctx_next_counter(vxl_ctx* ctx) { return ctx->d_counters + (ctx->counter_next++ % kCounterRing); }
 
 // glm::translate(m, v): Result[3] = m[0]*v[0] + m[1]*v[1] + m[2]*v[2] + m[3]
@@ -441,6 +458,28 @@ vxl_status vxl_trace_occlusion_host(vxl_ctx* ctx, const vxl_grid* g, const float
     if (npix == 0) return VXL_OK;
     VXL_TRY(set_device(ctx));
     cudaStream_t s = (cudaStream_t)stream;
+    // Pinned host memory is mapped into the device's address space; over the
+    // coherent CPU-GPU link the kernel then reads the G-buffer and writes the
+    // outputs in place, with no copy stages. Any other buffer (pageable memory)
+    // takes the staged copy pipeline below.
+    {
+        const float* in[3] = {h_pos, h_nrm, h_rough};
+        float* out[5] = {h_shadow, h_ao, h_ao_vis, h_spec, h_spec_t};
+        const float* din[3] = {nullptr, nullptr, nullptr};
+        float* dout[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+        bool mapped = true;
+        for (int k = 0; k < 3 && mapped; k++)
+            if (in[k]) mapped = device_view(ctx, in[k], (void**)&din[k]);
+        for (int k = 0; k < 5 && mapped; k++)
+            if (out[k]) mapped = device_view(ctx, out[k], (void**)&dout[k]);
+        if (mapped && occl_pool_supported(g, p)) {
+            vxl_gbuffer gb{din[0], din[1], din[2], npix, 0, 0};
+            vxl_outputs o{dout[0], dout[1], dout[2], dout[3], dout[4], nullptr};
+            VXL_TRY(launch_trace_occlusion(ctx, g, &gb, p, &o, s));
+            VXL_TRY_CUDA(cudaStreamSynchronize(s));
+            return VXL_OK;
+        }
+    }
     const size_t b3 = (size_t)npix * 3 * sizeof(float), b1 = (size_t)npix * sizeof(float);
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
     size_t need = 2 * al(b3) + 6 * al(b1);
