@@ -66,7 +66,9 @@ static bool device_view(const vxl_ctx* ctx, const void* h, void** d) {
         cudaGetLastError();  // clear the error of an unknown pointer
         return false;
     }
-    if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr) return false;
+    // pinned under this device's context (memory pinned for another device is
+    // not assumed to be mapped here)
+    if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr || a.device != ctx->device) return false;
     int mapped = 0;
     if (cudaDeviceGetAttribute(&mapped, cudaDevAttrCanMapHostMemory, ctx->device) != cudaSuccess || !mapped)
         return false;
