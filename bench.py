@@ -386,7 +386,8 @@ def run_gpu(args, wl):
     achieved = b_ray * rays_per_step / (ms / 1e3) / 1e9
     line = {
         "metric": "Grays/s shadow+AO+spec occlusion (exact voxel DDA)", "value": value, "unit": "Grays/s",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "ms_per_step_median": statistics.median(times), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene and G-buffer)",
         "config": config_dict(wl),
         "rays_per_step": rays_per_step, "valid_pixels": valid, "s_ref_mean_fetches_per_ray": s_ref,
