@@ -117,8 +117,10 @@ def test_occlusion_c1_bit_exact(vxl, ctx, n_spec):
 @pytest.mark.parametrize("scene,ao_len,shadow_len", [("boxes", 32.0, 100.0), ("boxes", 64.0, 130.0),
                                                      ("noise", 24.0, 60.0)])
 def test_occlusion_leap_matches_exact(vxl, ctx, scene, ao_len, shadow_len):
-    """Without per-ray records the kernel crosses empty bricks in one leap;
-    its buffers must equal the exact stepping (records mode) and the oracle."""
+    """With the leap enabled (tuning leap = 1) and no per-ray records, the
+    kernel crosses empty bricks in one leap; its buffers, those of the default
+    exact stepping (8-pixel tiles at 14 rays per pixel) and those of the
+    records mode must all equal the oracle."""
     import torch
 
     n, W, H = 192, 320, 200
@@ -137,7 +139,15 @@ def test_occlusion_leap_matches_exact(vxl, ctx, scene, ao_len, shadow_len):
     keys = ("shadow", "ao", "ao_vis", "spec", "spec_t")
     leap = {k: empty(npix, torch.float32) for k in keys}
     exact = {k: empty(npix, torch.float32) for k in keys}
-    vxl.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, **leap)
+    plain = {k: empty(npix, torch.float32) for k in keys}
+    before = ctx.get_tuning()
+    try:
+        ctx.set_tuning(leap=1)
+        vxl.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, **leap)
+        torch.cuda.synchronize()
+    finally:
+        ctx.set_tuning(**before)
+    vxl.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, **plain)
     vxl.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, records=rec_buffer(npix * 14), **exact)
     torch.cuda.synchronize()
     OP = oracle.make_params(light_dir=(-0.2, 0.9, 0.4), cam_pos=cam, n_ao=12, ao_len=ao_len, shadow_len=shadow_len,
@@ -146,6 +156,7 @@ def test_occlusion_leap_matches_exact(vxl, ctx, scene, ao_len, shadow_len):
     for k in keys:
         assert same_bits(leap[k].cpu().numpy(), exact[k].cpu().numpy()).all(), k
         assert same_bits(leap[k].cpu().numpy(), want[k]).all(), k
+        assert same_bits(plain[k].cpu().numpy(), want[k]).all(), k
     assert 0.0 < float(leap["shadow"].mean()) < 1.0
 
 
