@@ -531,6 +531,24 @@ vxl_status vxl_prefab_volume_at(const vxl_prefab* prefab, int i, int32_t* sx, in
 vxl_status vxl_prefab_palette_at(const vxl_prefab* prefab, int i, const uint8_t** h_materials, uint64_t* guid);
 vxl_status vxl_prefab_destroy(vxl_prefab* prefab);
 
+/* MagicaVoxel .vox import as the engine's importer does it
+ * (Sources/Editor/Importer/VoxImporter.cpp): one model per shape instance of
+ * the scene graph, in the importer's depth-first order, each with the name,
+ * size (a multiple of 4 per axis) and voxel bytes the importer writes to
+ * <name>.v, and the world position of its entity; and the 256-material
+ * palette (7 bytes each: r, g, b, a, roughness, metallic, emit) it writes to
+ * the .p file. Host memory, owned by the scene. */
+typedef struct vxl_vox_scene vxl_vox_scene;
+vxl_status vxl_vox_load(const char* path, vxl_vox_scene** out);
+vxl_status vxl_vox_info(const vxl_vox_scene* scene, int32_t* n_models);
+/* name: NUL-terminated, truncated to name_cap bytes; size: x, y, z of the
+ * .v file (data is x fastest, valid until vxl_vox_destroy); position: world
+ * units */
+vxl_status vxl_vox_model_at(const vxl_vox_scene* scene, int32_t i, char* name, int32_t name_cap, int32_t size[3],
+                            const uint8_t** h_data, float position[3]);
+vxl_status vxl_vox_palette(const vxl_vox_scene* scene, uint8_t* h_materials /* 256 * 7 bytes */);
+vxl_status vxl_vox_destroy(vxl_vox_scene* scene);
+
 /* .v asset reader (VoxAsset::Serialize, VoxAsset.h:42-50): u32 sx,sy,sz then
  * sx*sy*sz bytes. Query with data == NULL to get the sizes, then read into a
  * host buffer of sx*sy*sz bytes. */

@@ -44,6 +44,7 @@ EXPORTED = [
     "vxl_trace_soft_fwd", "vxl_trace_soft_bwd", "vxl_volume_build_mips", "vxl_trace_primary",
     "vxl_asset_guid", "vxl_read_palette", "vxl_transform_matrix", "vxl_prefab_load", "vxl_prefab_info",
     "vxl_prefab_renderer_at", "vxl_prefab_volume_at", "vxl_prefab_palette_at", "vxl_prefab_destroy",
+    "vxl_vox_load", "vxl_vox_info", "vxl_vox_model_at", "vxl_vox_palette", "vxl_vox_destroy",
     "vxl_read_v", "vxl_scene_soft", "vxl_scene_terrain", "vxl_scene_noise", "vxl_scene_boxes", "vxl_scene_gbuffer",
 ]
 
@@ -211,6 +212,12 @@ def lib():
         L.vxl_prefab_load.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(vp)]
         L.vxl_prefab_info.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L.vxl_prefab_renderer_at.argtypes = [vp, C.c_int, C.POINTER(PrefabRenderer)]
+        L.vxl_vox_load.argtypes = [C.c_char_p, C.POINTER(vp)]
+        L.vxl_vox_info.argtypes = [vp, C.POINTER(C.c_int32)]
+        L.vxl_vox_model_at.argtypes = [vp, C.c_int32, C.c_char_p, C.c_int32, C.POINTER(C.c_int32),
+                                       C.POINTER(C.POINTER(C.c_uint8)), C.POINTER(C.c_float)]
+        L.vxl_vox_palette.argtypes = [vp, C.POINTER(C.c_uint8)]
+        L.vxl_vox_destroy.argtypes = [vp]
         L.vxl_prefab_volume_at.argtypes = [vp, C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                            C.POINTER(C.c_int32), C.POINTER(C.POINTER(C.c_uint8)),
                                            C.POINTER(C.c_uint64)]
@@ -667,6 +674,32 @@ def transform_matrix(pos, rot, scale, parent=None) -> np.ndarray:
     check(lib().vxl_transform_matrix(p.ctypes.data, r.ctypes.data, s_.ctypes.data,
                                      None if par is None else par.ctypes.data, out.ctypes.data))
     return out
+
+
+def load_vox(path: str) -> dict:
+    """vxl_vox_load: a MagicaVoxel .vox file imported as the engine's importer
+    does: dict(models=[dict(name, volume=uint8 [sz, sy, sx], position=float32[3])],
+    palette=uint8 [256, 7])."""
+    h = C.c_void_p()
+    check(lib().vxl_vox_load(path.encode(), C.byref(h)))
+    try:
+        n = C.c_int32()
+        check(lib().vxl_vox_info(h, C.byref(n)))
+        models = []
+        for i in range(n.value):
+            name = C.create_string_buffer(256)
+            size = (C.c_int32 * 3)()
+            ptr = C.POINTER(C.c_uint8)()
+            pos = (C.c_float * 3)()
+            check(lib().vxl_vox_model_at(h, i, name, 256, size, C.byref(ptr), pos))
+            sx, sy, sz = size
+            vol = np.ctypeslib.as_array(ptr, (sx * sy * sz,)).copy().reshape(sz, sy, sx)
+            models.append(dict(name=name.value.decode(), volume=vol, position=np.array(pos, np.float32)))
+        pal = np.zeros(256 * 7, np.uint8)
+        check(lib().vxl_vox_palette(h, pal.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return dict(models=models, palette=pal.reshape(256, 7))
+    finally:
+        lib().vxl_vox_destroy(h)
 
 
 def load_prefab(mods_dir: str, mod_path: str) -> dict:
