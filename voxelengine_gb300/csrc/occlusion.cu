@@ -124,8 +124,10 @@ __device__ __forceinline__ bool tile_pixel(const SceneDesc& S, int64_t tile, int
 
 // Phases A-C for one tile of one scene.
 // HIT_T: the single-scene form: write a ray's t for hits only (the fold reads
-// no other) and step under one counter; the batched kernel keeps writing every
-// t and two counters, which its register allocation prefers
+// no other), step under one counter and leave out the bounds test where a
+// warp's next steps cannot reach the bounds; the batched kernel keeps writing
+// every t, two counters and the test at every step, which its register
+// allocation prefers
 template <int TP, int KSTEP, bool LEAP, bool RECORDS, bool HIT_T = false, bool CACHE = true>
 __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView& g, int64_t tile, PSlot* slots,
                                              float* res_t, uint32_t* res_hit, int lane) {
@@ -256,7 +258,7 @@ __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView&
         if (!__any_sync(0xffffffffu, busy) && base >= live) break;
         if (busy) {
             Hit h;
-            const int f = dda_run<LEAP, CACHE, HIT_T>(g, s, h, KSTEP);
+            const int f = dda_run<LEAP, CACHE, HIT_T, HIT_T>(g, s, h, KSTEP);
             if (f) {
                 const int k = (meta >> 9) & 31, pp = (meta >> 4) & 31;
                 if (!HIT_T || (f & VXL_RF_HIT)) res_t[k * TP + pp] = h.t;

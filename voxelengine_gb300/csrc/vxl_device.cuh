@@ -340,11 +340,13 @@ __device__ __forceinline__ bool dda_leap(DState& s) {
 // ONE_COUNT: the step budget and the 256-step cap share one limit, so a step
 // tests one counter (faster in the single-scene pool, slower in the batched
 // one, whose register allocation differs).
-template <bool LEAP = false, bool CACHE = true, bool ONE_COUNT = false>
-__device__ __forceinline__ int dda_run(const GridView& g, DState& s, Hit& r, int budget) {
+// CHECK: the bounds test of Light.frag:53-55 at every iteration; dda_run
+// leaves it out where no iteration of the call can reach the bounds.
+template <bool LEAP, bool CACHE, bool ONE_COUNT, bool CHECK>
+__device__ __forceinline__ int dda_steps(const GridView& g, DState& s, Hit& r, int budget) {
     const int lim = ONE_COUNT ? min(s.n + budget, 256) : 256;
     for (int it = 0; ONE_COUNT || it < budget; it++) {
-        if ((unsigned)s.cx > g.ux || (unsigned)s.cy > g.uy || (unsigned)s.cz > g.uz) {
+        if (CHECK && ((unsigned)s.cx > g.ux || (unsigned)s.cy > g.uy || (unsigned)s.cz > g.uz)) {
             r = Hit{s.cx, s.cy, s.cz, s.tot, s.n, VXL_RF_EXIT_BOUNDS};
             return VXL_RF_EXIT_BOUNDS;
         }
@@ -394,6 +396,28 @@ __device__ __forceinline__ int dda_run(const GridView& g, DState& s, Hit& r, int
         }
     }
     return 0;
+}
+
+// Without the leap an iteration moves the cell by at most one along each
+// axis, so from a cell within the bounds the next m + 1 iterations, m the
+// fewest cells to the bound along any axis's step direction, test cells within
+// the bounds too. With SKIP_BOUNDS, when that covers the budget for every
+// active lane of the warp, the warp steps without the bounds test; otherwise
+// it keeps the test at every iteration (a per-lane choice would run both loops
+// one after the other). Faster in the single-scene pool (+1% on L2-resident
+// grids, whose surface points lie near the bounds; +8% on a 2048^3 terrain),
+// slower in the batched kernel (-10%), which keeps the test.
+template <bool LEAP = false, bool CACHE = true, bool ONE_COUNT = false, bool SKIP_BOUNDS = false>
+__device__ __forceinline__ int dda_run(const GridView& g, DState& s, Hit& r, int budget) {
+    if (SKIP_BOUNDS && !LEAP) {
+        const int mx = s.sx > 0 ? (int)g.ux - s.cx : s.cx;
+        const int my = s.sy > 0 ? (int)g.uy - s.cy : s.cy;
+        const int mz = s.sz > 0 ? (int)g.uz - s.cz : s.cz;
+        const bool inside = (unsigned)s.cx <= g.ux && (unsigned)s.cy <= g.uy && (unsigned)s.cz <= g.uz;
+        const bool clear = inside && min(min(mx, my), mz) >= budget - 1;
+        if (__all_sync(__activemask(), clear)) return dda_steps<false, CACHE, ONE_COUNT, false>(g, s, r, budget);
+    }
+    return dda_steps<LEAP, CACHE, ONE_COUNT, true>(g, s, r, budget);
 }
 
 __device__ __forceinline__ Hit dda_fast(const GridView& g, f3 o, f3 d, float maxt) {
