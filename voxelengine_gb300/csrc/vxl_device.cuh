@@ -340,13 +340,11 @@ __device__ __forceinline__ bool dda_leap(DState& s) {
 // ONE_COUNT: the step budget and the 256-step cap share one limit, so a step
 // tests one counter (faster in the single-scene pool, slower in the batched
 // one, whose register allocation differs).
-// CHECK: the bounds test of Light.frag:53-55 at every iteration; dda_run
-// leaves it out where no iteration of the call can reach the bounds.
-template <bool LEAP, bool CACHE, bool ONE_COUNT, bool CHECK>
+template <bool LEAP, bool CACHE, bool ONE_COUNT>
 __device__ __forceinline__ int dda_steps(const GridView& g, DState& s, Hit& r, int budget) {
     const int lim = ONE_COUNT ? min(s.n + budget, 256) : 256;
     for (int it = 0; ONE_COUNT || it < budget; it++) {
-        if (CHECK && ((unsigned)s.cx > g.ux || (unsigned)s.cy > g.uy || (unsigned)s.cz > g.uz)) {
+        if ((unsigned)s.cx > g.ux || (unsigned)s.cy > g.uy || (unsigned)s.cz > g.uz) {
             r = Hit{s.cx, s.cy, s.cz, s.tot, s.n, VXL_RF_EXIT_BOUNDS};
             return VXL_RF_EXIT_BOUNDS;
         }
@@ -398,15 +396,61 @@ __device__ __forceinline__ int dda_steps(const GridView& g, DState& s, Hit& r, i
     return 0;
 }
 
+// `budget` iterations that can meet neither the bounds nor the 256-step cap
+// (the caller has checked both for the whole budget): only a hit or
+// totalt >= maxt ends the ray early, the step count follows the iteration
+// index, and with a compile-time budget the loop unrolls without a counter.
+template <bool CACHE>
+__device__ __forceinline__ int dda_steps_clear(const GridView& g, DState& s, Hit& r, int budget) {
+#pragma unroll
+    for (int it = 0; it < budget; it++) {
+        uint64_t word;
+        if (CACHE) {
+            const uint32_t wi = word_index(g, s.cx, s.cy, s.cz);
+            if (wi != s.wcur) {
+                s.wcur = wi;
+                s.word = __ldg(g.words + wi);
+            }
+            word = s.word;
+        } else {
+            word = __ldg(g.words + word_index(g, s.cx, s.cy, s.cz));
+        }
+        const float m = fminf(fminf(s.tx, s.ty), s.tz);
+        const bool bx = s.tx == m, by = s.ty == m, bz = s.tz == m;
+        float best = m + 0.0f;
+        if ((bx && (by || bz)) || (by && bz)) {
+            best = (bx ? s.tx : 0.0f) + (by ? s.ty : 0.0f);
+            best = best + (bz ? s.tz : 0.0f);
+        }
+        if ((word >> bit_index(s.cx, s.cy, s.cz)) & 1ull) {
+            const int f = VXL_RF_HIT | (bx ? VXL_RF_SELX : 0) | (by ? VXL_RF_SELY : 0) | (bz ? VXL_RF_SELZ : 0);
+            r = Hit{s.cx, s.cy, s.cz, best, s.n + it + 1, f};
+            return f;
+        }
+        const int px = s.cx, py = s.cy, pz = s.cz;
+        if (bx) { s.cx += s.sx; s.tx = s.tx + s.tdx; }
+        if (by) { s.cy += s.sy; s.ty = s.ty + s.tdy; }
+        if (bz) { s.cz += s.sz; s.tz = s.tz + s.tdz; }
+        s.tot = best;
+        if (!(best < s.maxt)) {
+            s.n += it + 1;
+            r = Hit{px, py, pz, best, s.n, VXL_RF_EXIT_MAXT};
+            return VXL_RF_EXIT_MAXT;
+        }
+    }
+    s.n += budget;
+    return 0;
+}
+
 // Without the leap an iteration moves the cell by at most one along each
 // axis, so from a cell within the bounds the next m + 1 iterations, m the
 // fewest cells to the bound along any axis's step direction, test cells within
 // the bounds too. With SKIP_BOUNDS, when that covers the budget for every
-// active lane of the warp, the warp steps without the bounds test; otherwise
-// it keeps the test at every iteration (a per-lane choice would run both loops
-// one after the other). Faster in the single-scene pool (+1% on L2-resident
-// grids, whose surface points lie near the bounds; +8% on a 2048^3 terrain),
-// slower in the batched kernel (-10%), which keeps the test.
+// active lane of the warp and no lane can reach the 256-step cap in it, the
+// warp runs the budget without the bounds test and the step counter;
+// otherwise it keeps both at every iteration (a per-lane choice would run both
+// loops one after the other). Faster in the single-scene pool, slower in the
+// batched kernel (-10%), which keeps the tests.
 template <bool LEAP = false, bool CACHE = true, bool ONE_COUNT = false, bool SKIP_BOUNDS = false>
 __device__ __forceinline__ int dda_run(const GridView& g, DState& s, Hit& r, int budget) {
     if (SKIP_BOUNDS && !LEAP) {
@@ -414,10 +458,10 @@ __device__ __forceinline__ int dda_run(const GridView& g, DState& s, Hit& r, int
         const int my = s.sy > 0 ? (int)g.uy - s.cy : s.cy;
         const int mz = s.sz > 0 ? (int)g.uz - s.cz : s.cz;
         const bool inside = (unsigned)s.cx <= g.ux && (unsigned)s.cy <= g.uy && (unsigned)s.cz <= g.uz;
-        const bool clear = inside && min(min(mx, my), mz) >= budget - 1;
-        if (__all_sync(__activemask(), clear)) return dda_steps<false, CACHE, ONE_COUNT, false>(g, s, r, budget);
+        const bool clear = inside && min(min(mx, my), mz) >= budget - 1 && s.n + budget < 256;
+        if (__all_sync(__activemask(), clear)) return dda_steps_clear<CACHE>(g, s, r, budget);
     }
-    return dda_steps<LEAP, CACHE, ONE_COUNT, true>(g, s, r, budget);
+    return dda_steps<LEAP, CACHE, ONE_COUNT>(g, s, r, budget);
 }
 
 __device__ __forceinline__ Hit dda_fast(const GridView& g, f3 o, f3 d, float maxt) {
