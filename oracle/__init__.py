@@ -145,6 +145,9 @@ def lib():
                                             C.POINTER(C.c_uint32), ip]
             L.vo_affine_inverse.argtypes = [fp, fp, fp]
             L.vo_rebuild_from_depth.argtypes = [fp, fp, C.c_int, C.c_int, fp, fp, fp, fp]
+            L.vo_ray_vox_cast.argtypes = [u8p, C.c_int, C.c_int, C.c_int, fp, fp, fp, fp,
+                                          C.POINTER(C.c_int), C.POINTER(C.c_int)]
+            L.vo_ray_vox_cast.restype = C.c_int
             L.vo_primary.argtypes = [vp, vp, vp, ip, fp, ip, C.c_int, fp, fp, C.c_float, C.c_int, C.c_int, C.c_int,
                                      fp, fp, fp, ip, ip, C.c_int]
             L.vo_taa.argtypes = [fp, fp, fp, fp, fp, fp, fp, fp, C.c_int, C.c_int, fp, C.c_int]
@@ -489,6 +492,24 @@ def rebuild_from_depth(depth, nrm, W, H, inv_view, inv_proj):
     n2 = np.zeros((W * H, 3), np.float32)
     lib().vo_rebuild_from_depth(_f(depth), _f(nrm), W, H, _f(iv), _f(ip), _f(wcp), _f(n2))
     return wcp, n2
+
+
+def ray_vox_cast(model, inv_obb, ray_pos, ray_dir):
+    """The engine's picking DDA (vo_ray_vox_cast) against one model, a
+    uint8[sz, sy, sx] array. inv_obb: the inverse of the model's world matrix,
+    float32[16] column-major. Returns (hit, t, cell[3], iterations)."""
+    model = np.ascontiguousarray(model, np.uint8)
+    msz, msy, msx = model.shape
+    inv = np.ascontiguousarray(inv_obb, np.float32).reshape(16)
+    p = np.ascontiguousarray(ray_pos, np.float32).reshape(3)
+    d = np.ascontiguousarray(ray_dir, np.float32).reshape(3)
+    t = np.zeros(1, np.float32)
+    cell = np.zeros(3, np.int32)
+    it = np.zeros(1, np.int32)
+    ip = C.POINTER(C.c_int)
+    hit = lib().vo_ray_vox_cast(model.ctypes.data_as(C.POINTER(C.c_uint8)), msx, msy, msz, _f(inv), _f(p), _f(d),
+                                _f(t), cell.ctypes.data_as(ip), it.ctypes.data_as(ip))
+    return bool(hit), float(t[0]), cell, int(it[0])
 
 
 def primary(volumes, worlds, vol_of, cam, target, W, H, frame=0, tan_half_fov=0.57735026, threads=None):

@@ -23,7 +23,9 @@ output into oracle/_ref/ (git-ignored):
   VoxAsset::Upload (Sources/Asset/VoxAsset.cpp) is cut out and compiled there too.
 * TransformSystem::RealculateMatrix (Sources/World/Systems/TransformSystem.cpp)
   is cut out, made a free function, and compiled in ref_transform_harness.cpp
-  against the vendored glm.
+  against the vendored glm; so is the picking DDA RayVoxCast
+  (Sources/World/Systems/PhysicsSystem.cpp), unmodified, with stand-ins for
+  the engine's asset reference and VoxAsset::PixelAt.
 * main and luminance of Sources/Shaders/LightTAA.frag are cut out (main renamed
   taa_main; assignments to a .xyz swizzle rewritten component-wise) and
   compiled in ref_taa_harness.cpp with the library's bilinear sampler.
@@ -121,6 +123,7 @@ def generate() -> None:
     geo = open(os.path.join(sh, "GeometryVoxel.frag")).read()
     voxasset = open(os.path.join(r, "Sources", "Asset", "VoxAsset.cpp")).read()
     transform = open(os.path.join(r, "Sources", "World", "Systems", "TransformSystem.cpp")).read()
+    physics = open(os.path.join(r, "Sources", "World", "Systems", "PhysicsSystem.cpp")).read()
     taa = open(os.path.join(sh, "LightTAA.frag")).read()
     parts = {
         "geometry_clip.inc": _glslpp(_function(geo, "vec3 clipToAABB(")),
@@ -131,6 +134,7 @@ def generate() -> None:
                                                                                          "void taa_main()", 1))),
         "transform_realculate.inc": _function(transform, "void TransformSystem::RealculateMatrix(").replace(
             "TransformSystem::", "", 1),
+        "physics_rayvox.inc": _function(physics, "bool RayVoxCast("),
         "Light_frag.inc": _glslpp(light),
         "ambient_cosine.inc": _glslpp(_function(amb, "vec3 cosineSampleHemisphere(")),
         "ambient_irradiance.inc": _glslpp(_function(amb, "vec3 calculateAmbientIrradiance(")),

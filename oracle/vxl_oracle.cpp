@@ -1594,3 +1594,79 @@ void vo_rebuild_from_depth(const float* depth, const float* nrm, int W, int H, c
             n[2] = nrm[3 * k + 2];
         }
 }
+
+// ---------------------------------------------------------------------------
+// RayVoxCast, Sources/World/Systems/PhysicsSystem.cpp:98-145: the engine's own
+// CPU DDA, used for picking one placed model. It is a second meaning of
+// "voxel DDA", next to raycastShadowVolume:
+// * it steps before it tests, so the origin cell is never tested;
+// * it leaves at the first cell outside [0, size-1];
+// * it runs at most 257 iterations (`do ... while (i++ < 256)`);
+// * it nudges zero direction components to 1e-8;
+// * a hit reports the entry time of the hit cell, dot(tMax, select) * 0.1.
+// Host C++ compiled against glm, so the arithmetic order is glm's: mat4 * vec4
+// adds the column terms pairwise, (c0*x + c1*y) + (c2*z + c3*w), and dot adds
+// left to right. inv_obb is glm::inverse(obb), column-major, supplied by the
+// caller (the cofactor inverse is not restated here). The model is 1 byte per
+// voxel, x fastest (VoxAsset::PixelAt, Sources/Asset/VoxAsset.h:52-56), and
+// obbSize is the model size.
+static void glm_mat4_vec(const float* m, float x, float y, float z, float w, float* o) {
+    for (int r = 0; r < 4; r++) {
+        const float a0 = m[r] * x + m[4 + r] * y;
+        const float a1 = m[8 + r] * z + m[12 + r] * w;
+        o[r] = a0 + a1;
+    }
+}
+
+int vo_ray_vox_cast(const uint8_t* model, int msx, int msy, int msz, const float* inv_obb, const float* ray_pos,
+                    const float* ray_dir, float* t_out, int* cell_out, int* iters_out) {
+    float lp[4], ld[4], m[16];
+    glm_mat4_vec(inv_obb, ray_pos[0], ray_pos[1], ray_pos[2], 1.0f, lp);
+    const V3 localPos = v3(lp[0] * 10.0f, lp[1] * 10.0f, lp[2] * 10.0f);
+    std::memcpy(m, inv_obb, sizeof(m));
+    m[12] = 0.0f;  // invObb[3] = vec4(0, 0, 0, 1)
+    m[13] = 0.0f;
+    m[14] = 0.0f;
+    m[15] = 1.0f;
+    glm_mat4_vec(m, ray_dir[0], ray_dir[1], ray_dir[2], 0.0f, ld);
+    V3 localDir = v3(ld[0], ld[1], ld[2]);
+    if (localDir.x == 0.0f) localDir.x = 0.00000001f;
+    if (localDir.y == 0.0f) localDir.y = 0.00000001f;
+    if (localDir.z == 0.0f) localDir.z = 0.00000001f;
+    const V3 stepSign = v3(glsl_sign(localDir.x), glsl_sign(localDir.y), glsl_sign(localDir.z));
+    const V3 tDelta = v3(1.0f / (localDir.x * stepSign.x), 1.0f / (localDir.y * stepSign.y),
+                         1.0f / (localDir.z * stepSign.z));
+    int cx = (int)std::floor(localPos.x), cy = (int)std::floor(localPos.y), cz = (int)std::floor(localPos.z);
+    const V3 nb = v3((float)cx + (stepSign.x * 0.5f + 0.5f), (float)cy + (stepSign.y * 0.5f + 0.5f),
+                     (float)cz + (stepSign.z * 0.5f + 0.5f));
+    V3 tMax = v3((nb.x - localPos.x) / localDir.x, (nb.y - localPos.y) / localDir.y,
+                 (nb.z - localPos.z) / localDir.z);
+    int i = 0;
+    do {
+        // step(tMax, tMax.zxy) * step(tMax, tMax.yzx)
+        const float sx = glsl_step(tMax.x, tMax.z) * glsl_step(tMax.x, tMax.y);
+        const float sy = glsl_step(tMax.y, tMax.x) * glsl_step(tMax.y, tMax.z);
+        const float sz = glsl_step(tMax.z, tMax.y) * glsl_step(tMax.z, tMax.x);
+        cx += (int)(sx * stepSign.x);
+        cy += (int)(sy * stepSign.y);
+        cz += (int)(sz * stepSign.z);
+        if (iters_out) *iters_out = i + 1;
+        if (cell_out) {
+            cell_out[0] = cx;
+            cell_out[1] = cy;
+            cell_out[2] = cz;
+        }
+        if (cx < 0 || cy < 0 || cz < 0 || cx > msx - 1 || cy > msy - 1 || cz > msz - 1) return 0;
+        const uint8_t voxel = model[(size_t)cx + (size_t)cy * msx + (size_t)cz * msx * msy];
+        if (voxel != 0) {
+            float d = tMax.x * sx + tMax.y * sy;
+            d = d + tMax.z * sz;
+            if (t_out) *t_out = d * 0.1f;
+            return 1;
+        }
+        tMax.x += tDelta.x * sx;
+        tMax.y += tDelta.y * sy;
+        tMax.z += tDelta.z * sz;
+    } while (i++ < 256);
+    return 0;
+}

@@ -169,6 +169,14 @@ void vo_primary(const uint8_t* const* mip0s, const uint8_t* const* mip1s, const 
 void vo_rebuild_from_depth(const float* depth, const float* nrm, int W, int H, const float* inv_view,
                            const float* inv_proj, float* wcp, float* nrm_out);
 
+/* RayVoxCast (Sources/World/Systems/PhysicsSystem.cpp:98-145), the engine's
+ * picking DDA against one model of msx*msy*msz bytes (x fastest). inv_obb is
+ * glm::inverse(obb), column-major; the ray is in world units. Returns 1 on a
+ * hit with *t_out = entry time * 0.1; cell_out = the last cell reached (the
+ * hit cell, or the first one outside the model); iters_out = iterations run. */
+int vo_ray_vox_cast(const uint8_t* model, int msx, int msy, int msz, const float* inv_obb, const float* ray_pos,
+                    const float* ray_dir, float* t_out, int* cell_out, int* iters_out);
+
 #ifdef __cplusplus
 }
 #endif

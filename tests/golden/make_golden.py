@@ -2,7 +2,8 @@
 this machine (oracle/ref/build_ref.py -> oracle/_ref/libvxl_ref.so).
 
 Run: python tests/golden/make_golden.py   (needs the VoxelEngine tree at
-/root/reference or $VXL_REFERENCE_DIR). The fixtures let the oracle be checked
+/root/reference or $VXL_REFERENCE_DIR); `python tests/golden/make_golden.py
+rayvox` writes only rayvox.npz. The fixtures let the oracle be checked
 against the reference where the reference tree is absent.
 """
 import ctypes as C
@@ -146,8 +147,36 @@ def main():
                             volume_shapes=np.array([v.shape for v in vols], np.int32),
                             vol_of=np.array([guids.index(r[2]) for r in rens], np.int32), world=worlds,
                             pivot=pivots, matrix=mats, palette=pal)
+    make_rayvox(R)
     print("golden fixtures written to", HERE)
 
 
+def make_rayvox(R):
+    """RayVoxCast (PhysicsSystem.cpp:98-145) on seeded models, placements and
+    picking rays, with glm's inverse of each placement beside it."""
+    rng = np.random.default_rng(31)
+    models = [vox_cases.random_model(rng, *rng.integers(2, 9, 3) * 4, fill=f) for f in (0.3, 0.08, 0.5, 0.02)]
+    cases = vox_cases.rayvox_cases(rng, [m.shape for m in models], n_per_model=150)
+    n = len(cases)
+    inv = np.zeros((n, 16), np.float32)
+    hit = np.zeros(n, np.int32)
+    t = np.zeros(n, np.float32)
+    for i, (mi, obb, p, d) in enumerate(cases):
+        m = np.ascontiguousarray(models[mi])
+        sz, sy, sx = m.shape
+        R.ref_glm_inverse(f(obb), inv[i].ctypes.data_as(fp))
+        tt = np.zeros(1, np.float32)
+        hit[i] = R.ref_ray_vox_cast(f(obb), m.ctypes.data_as(u8), sx, sy, sz, f(p), f(d), tt.ctypes.data_as(fp))
+        t[i] = tt[0]
+    np.savez_compressed(os.path.join(HERE, "rayvox.npz"), models=np.concatenate([m.reshape(-1) for m in models]),
+                        model_shapes=np.array([m.shape for m in models], np.int32),
+                        model_of=np.array([c[0] for c in cases], np.int32), obb=np.stack([c[1] for c in cases]),
+                        pos=np.stack([c[2] for c in cases]), dir=np.stack([c[3] for c in cases]), inv=inv, hit=hit,
+                        t=t)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["rayvox"]:
+        make_rayvox(bind(C.CDLL(build_ref.build()), oracle))
+    else:
+        main()

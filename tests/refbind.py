@@ -30,6 +30,9 @@ def bind(R, oracle_lib):
     R.ref_vox_update.argtypes = [ip, C.c_int]
     R.ref_vox_destroy.argtypes = [C.c_int]
     R.ref_vox_flush.argtypes = [ip, C.c_int]
+    R.ref_ray_vox_cast.restype = C.c_int
+    R.ref_ray_vox_cast.argtypes = [fp, u8, C.c_int, C.c_int, C.c_int, fp, fp, fp]
+    R.ref_glm_inverse.argtypes = [fp, fp]
     R.ref_set_sincos.argtypes = [C.c_void_p]
     R.ref_set_sincos(C.cast(oracle_lib.lib().vo_sincos, C.c_void_p))
     return R

@@ -49,3 +49,28 @@ def farmhouse_models(ref_root=None, limit=12):
         return []
     names = sorted(os.listdir(d), key=lambda s: int(s.split(".")[0]) if s.split(".")[0].isdigit() else 1 << 30)
     return [read_v(os.path.join(d, n)) for n in names if n.endswith(".v")][:limit]
+
+
+def rayvox_cases(rng, shapes, n_per_model=400):
+    """Seeded picking rays for RayVoxCast: (model index, obb float32[16]
+    column-major, world origin float32[3], world direction float32[3]).
+    The obb is a rigid placement (identity rotation for a quarter of the
+    models, so that axis-aligned directions keep exact zero components and
+    take the 1e-8 nudge); origins lie in and around the model's box
+    (local cells -2 .. size+2, mapped by obb at 0.1 world units per cell)."""
+    out = []
+    for mi, (sz, sy, sx) in enumerate(shapes):
+        plain = mi % 4 == 0
+        obb = world_matrix(rng, -3.0, 3.0, rotate=not plain)
+        M = obb.reshape(4, 4).T.astype(np.float64)
+        for j in range(n_per_model):
+            local = rng.uniform(-2.0, 1.0, 3) + rng.uniform(0.0, 1.0, 3) * (np.array([sx, sy, sz]) + 2.0)
+            world = (M @ np.append(local * 0.1, 1.0))[:3]
+            if plain and j % 5 == 0:
+                d = np.zeros(3)
+                d[j % 3] = 1.0 if (j // 3) % 2 == 0 else -1.0
+            else:
+                d = rng.normal(size=3)
+                d /= np.linalg.norm(d)
+            out.append((mi, obb, world.astype(np.float32), d.astype(np.float32)))
+    return out
