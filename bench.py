@@ -180,11 +180,15 @@ def sum_over_ranks(dist, x):
 
 
 # --------------------------------------------------------------- CPU oracle
-def cpu_sample_rays_per_s(g_r8, pos, nrm, rough, P, W, H, budget_s=12.0, threads=None, band=32):
+def cpu_sample_rays_per_s(g_r8, pos, nrm, rough, P, W, H, budget_s=12.0, threads=None, band=32, against=None):
     """Time the oracle on bands of `band` whole image rows, taken in seeded
-    random order, until about budget_s of wall time (one oracle call per band,
-    so thread start-up is paid per band rather than per row); returns
-    (rays/s, rows, seconds, threads)."""
+    random order, until about budget_s of oracle time (one oracle call per
+    band, so thread start-up is paid per band rather than per row). With
+    `against` (the CUDA path's output buffers for the same frame, as numpy
+    arrays) each band's oracle outputs are also compared with them, outside
+    the timed calls. Returns (rays/s, rows, seconds, threads, check): check is
+    None without `against`, else the values compared, those whose bits differ
+    (any NaN equals any NaN) and the largest absolute difference."""
     import oracle
 
     threads = threads or (os.cpu_count() or 1)
@@ -194,17 +198,31 @@ def cpu_sample_rays_per_s(g_r8, pos, nrm, rough, P, W, H, budget_s=12.0, threads
     order = np.random.default_rng(1).permutation(len(starts))
     rays = 0
     rows = 0
-    t0 = time.perf_counter()
+    busy = 0.0
+    check = None if against is None else {"outputs": sorted(against), "values": 0, "bit_mismatches": 0,
+                                          "max_abs_diff": 0.0}
     for b in order:
         y0 = int(starts[b])
         y1 = min(H, y0 + band)
-        oracle.occlusion(g_r8, pos, nrm, rough, P, p0=y0 * W, p1=y1 * W, threads=threads)
+        t1 = time.perf_counter()
+        o = oracle.occlusion(g_r8, pos, nrm, rough, P, p0=y0 * W, p1=y1 * W, threads=threads)
+        busy += time.perf_counter() - t1
         rays += int(valid[y0:y1].sum()) * R
         rows += y1 - y0
-        if time.perf_counter() - t0 > budget_s:
+        if against is not None:
+            for k, gpu in against.items():
+                a = np.asarray(gpu[y0 * W:y1 * W], np.float32)
+                w = o[k][y0 * W:y1 * W]
+                both_nan = np.isnan(a) & np.isnan(w)
+                differ = (a.view(np.int32) != w.view(np.int32)) & ~both_nan
+                check["values"] += a.size
+                check["bit_mismatches"] += int(differ.sum())
+                d = np.abs(a.astype(np.float64) - w.astype(np.float64))[~(np.isnan(a) | np.isnan(w))]
+                if d.size:
+                    check["max_abs_diff"] = max(check["max_abs_diff"], float(d.max()))
+        if busy > budget_s:
             break
-    dt = time.perf_counter() - t0
-    return rays / dt, rows, dt, threads
+    return rays / busy, rows, busy, threads, check
 
 
 def run_reference(args, wl):
@@ -233,7 +251,7 @@ def run_reference(args, wl):
     # each step is a bounded sample; the whole run stays within ~150 s of CPU work
     budget = min(args.ref_step_seconds, 150.0 / max(1, args.warmup + args.steps))
     for s in range(args.warmup + args.steps):
-        v, rows, dt, th = cpu_sample_rays_per_s(g, pos, nrm, rough, P, W, H, budget_s=budget, threads=threads)
+        v, rows, dt, th, _ = cpu_sample_rays_per_s(g, pos, nrm, rough, P, W, H, budget_s=budget, threads=threads)
         if s >= args.warmup:
             per_step.append((v, rows, dt))
     rays_s = sum(v * dt for v, _, dt in per_step) / sum(dt for _, _, dt in per_step)
@@ -416,12 +434,15 @@ def run_gpu(args, wl):
         import oracle
 
         OP = oracle.make_params(cam_pos=cam, **P_kw)
-        v, rows, dt, th = cpu_sample_rays_per_s(g_np, pos.cpu().numpy(), nrm.cpu().numpy(), rough.cpu().numpy(), OP,
-                                                W, H, budget_s=args.cpu_seconds)
+        gpu_out = {k: t.cpu().numpy() for k, t in outs.items()}
+        v, rows, dt, th, chk = cpu_sample_rays_per_s(g_np, pos.cpu().numpy(), nrm.cpu().numpy(), rough.cpu().numpy(),
+                                                     OP, W, H, budget_s=args.cpu_seconds, against=gpu_out)
+        # the error against the CPU oracle on the sampled rows (bit-exact is expected)
+        line["oracle_check"] = dict(chk, sample="the cpu_baseline rows")
         line["cpu_baseline"] = {"value": v / 1e9, "unit": "Grays/s", "cores": th, "kind": "port",
                                 "sample": "%d whole image rows of %d in bands of 32, seeded random order (%.1f s), %d rays/px" % (
                                     rows, H, dt, R)}
-        v1, rows1, dt1, _ = cpu_sample_rays_per_s(g_np, pos.cpu().numpy(), nrm.cpu().numpy(),
+        v1, rows1, dt1, _, _ = cpu_sample_rays_per_s(g_np, pos.cpu().numpy(), nrm.cpu().numpy(),
                                                   rough.cpu().numpy(), OP, W, H,
                                                   budget_s=min(4.0, args.cpu_seconds), threads=1)
         line["cpu_baseline"]["one_core"] = {"value": v1 / 1e9, "unit": "Grays/s", "cores": 1,
