@@ -124,9 +124,10 @@ __device__ __forceinline__ bool tile_pixel(const SceneDesc& S, int64_t tile, int
 
 // Phases A-C for one tile of one scene.
 // HIT_T: the single-scene form: write a ray's t for hits only (the fold reads
-// no other), step under one counter and leave out the bounds test where a
-// warp's next steps cannot reach the bounds; the batched kernel keeps writing
-// every t, two counters and the test at every step, which its register
+// no other), step under one counter, and run a warp's KSTEP steps unrolled
+// without the bounds test and the counter where none of its lanes can reach
+// the bounds or the 256-step cap in them; the batched kernel keeps writing
+// every t, two counters and both tests at every step, which its register
 // allocation prefers
 template <int TP, int KSTEP, bool LEAP, bool RECORDS, bool HIT_T = false, bool CACHE = true>
 __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView& g, int64_t tile, PSlot* slots,
