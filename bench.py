@@ -225,6 +225,27 @@ def cpu_sample_rays_per_s(g_r8, pos, nrm, rough, P, W, H, budget_s=12.0, threads
     return rays / busy, rows, busy, threads, check
 
 
+def oracle_s_ref(g_r8, pos, nrm, rough, P, W, H, every=8, band=32, threads=None):
+    """Mean reference-DDA fetches per ray (S_ref) from the oracle's records
+    on a stratified sample: every `every`-th band of `band` image rows, over
+    the pixels that see geometry. Returns (S_ref, rows)."""
+    import oracle
+
+    R = P.n_shadow + P.n_ao + P.n_spec
+    valid = np.abs(nrm).reshape(-1, 3).sum(1) > 0
+    steps = 0
+    rays = 0
+    rows = 0
+    for y0 in range(0, H, band * every):
+        y1 = min(H, y0 + band)
+        o = oracle.occlusion_range(g_r8, pos, nrm, rough, P, y0 * W, y1 * W, threads=threads)
+        st = o["recs"]["steps"].reshape(-1, R)[valid[y0 * W:y1 * W]]
+        steps += int(st.sum())
+        rays += st.size
+        rows += y1 - y0
+    return steps / max(rays, 1), rows
+
+
 def run_reference(args, wl):
     """--impl reference: the oracle port on the host cores (no GPU work)."""
     import oracle
@@ -439,6 +460,9 @@ def run_gpu(args, wl):
                                                      OP, W, H, budget_s=args.cpu_seconds, against=gpu_out)
         # the error against the CPU oracle on the sampled rows (bit-exact is expected)
         line["oracle_check"] = dict(chk, sample="the cpu_baseline rows")
+        sref, srows = oracle_s_ref(g_np, pos.cpu().numpy(), nrm.cpu().numpy(), rough.cpu().numpy(), OP, W, H)
+        line["oracle_check"]["s_ref_oracle"] = sref
+        line["oracle_check"]["s_ref_sample"] = "oracle records of every 8th band of 32 rows: %d of %d rows" % (srows, H)
         line["cpu_baseline"] = {"value": v / 1e9, "unit": "Grays/s", "cores": th, "kind": "port",
                                 "sample": "%d whole image rows of %d in bands of 32, seeded random order (%.1f s), %d rays/px" % (
                                     rows, H, dt, R)}

@@ -35,3 +35,21 @@ def test_cpu_leg_compares_each_sampled_band():
     assert chk2["bit_mismatches"] == 1 and abs(chk2["max_abs_diff"] - 0.25) < 1e-6
     _, _, _, _, none = bench.cpu_sample_rays_per_s(g, pos, nrm, rough, P, W, H, budget_s=60.0, threads=2, band=32)
     assert none is None
+
+
+def test_oracle_s_ref_is_the_records_mean():
+    import bench
+
+    n, W, H = 32, 20, 300
+    g = oracle.scene_noise(n, n, n, seed=6, threads=2)
+    cam, tgt = bench.camera(n)
+    pos, nrm, rough = oracle.gbuffer(g, cam, tgt, W, H, 6, threads=2)
+    P = oracle.make_params(light_dir=bench.light_dir(6), cam_pos=cam, n_ao=4, ao_len=16.0, n_spec=1, seed=6)
+    full = oracle.occlusion(g, pos, nrm, rough, P, with_recs=True, threads=2)
+    R = 6
+    valid = np.abs(nrm).reshape(-1, 3).sum(1) > 0
+    rows = [y for y in range(H) if (y // 32) % 8 == 0]
+    pix = np.array([y * W + x for y in rows for x in range(W)])
+    steps = full["recs"]["steps"].reshape(-1, R)[pix[valid[pix]]]
+    sref, nrows = bench.oracle_s_ref(g, pos, nrm, rough, P, W, H, threads=2)
+    assert nrows == len(rows) == 64 and sref == steps.sum() / steps.size
