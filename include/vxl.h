@@ -14,6 +14,28 @@
  *    0.1 world units (Sources/World/Systems/ShadowVoxSystem.cpp:147, x10).
  *  - A grid of fine dimensions (nx,ny,nz) corresponds to the reference's R8
  *    ShadowVox image of (nx/2, ny/2, nz/2) bytes, 2x2x2 voxels per byte.
+ *  - Stream capture (CUDA graphs). Some calls only enqueue kernels and
+ *    memsets on `stream`: they neither synchronize, nor allocate, nor read
+ *    results back to the host. These may be captured:
+ *      - vxl_trace_rays, vxl_trace_occlusion, vxl_light_ambient,
+ *        vxl_light_reflection, vxl_light_point;
+ *      - vxl_trace_soft_fwd, vxl_trace_soft_bwd, vxl_volume_build_mips;
+ *      - vxl_grid_clear, vxl_grid_build_bricks, vxl_grid_import_r8,
+ *        vxl_grid_export_r8, vxl_grid_import_palette;
+ *      - vxl_scene_noise, vxl_scene_boxes, vxl_scene_soft, vxl_scene_gbuffer;
+ *      - vxl_batch_run of a batch created with use_graph = 0 (with
+ *        use_graph = 1 the batch replays its own graph).
+ *    A second group grows a context workspace the first time it sees a
+ *    larger frame. These may be captured only after an uncaptured call of
+ *    the same or a larger size on that context: vxl_trace_occlusion_from_depth,
+ *    vxl_light_points, vxl_light_taa, vxl_scene_terrain.
+ *    The rest must not be captured:
+ *      - vxl_trace_primary reads its tile-list total back to the host;
+ *      - the voxelizer calls upload host tables and wait for them;
+ *      - vxl_trace_occlusion_host and vxl_grid_count are synchronous;
+ *      - the create and destroy calls allocate or free.
+ *    A captured call fixes its scalar arguments and pointers in the graph,
+ *    and replays of one graph must not overlap.
  */
 #ifndef VXL_H
 #define VXL_H
