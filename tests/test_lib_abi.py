@@ -58,6 +58,22 @@ def test_null_arguments_are_rejected_without_device_work(V):
     assert L.vxl_voxelize_noalloc(None, None, 0, None, 0, None, None) == 1
 
 
+def test_context_on_a_missing_device_fails_with_a_status(V):
+    """Failure on the host, no GPU fault: a context on a device that does not
+    exist comes back as a status and a message (no exception across the ABI,
+    no context). Without a GPU the device count itself fails (VXL_ERR_CUDA);
+    with one, the index is out of range (VXL_ERR_INVALID_ARG)."""
+    import ctypes as C
+
+    L = V.lib()
+    out = C.c_void_p(12345)
+    st = L.vxl_ctx_create(1000, C.byref(out))
+    assert st in (1, 3), st
+    assert out.value is None
+    msg = L.vxl_last_error_string()
+    assert msg and (b"device" in msg or b"cuda" in msg.lower())
+
+
 def test_read_v_fixture_and_errors(V, tmp_path):
     from tests import vox_cases
 
