@@ -8,7 +8,10 @@ fractions, so every face-crossing time is exact.
   inclusive +1 over-bound exit.
 * raycastShadowVolumeSparse (Light.frag:131-173): the fine bit is chosen by
   mod(pos, 0.5) > 0.25, not by the cell the sample lies in.
-* getVolumeAt (Light.frag:14-27): integer division truncates toward zero."""
+* getVolumeAt (Light.frag:14-27): integer division truncates toward zero.
+* ShadowVoxSystem::OnUpdate / SetVolumeAt (ShadowVoxSystem.cpp:82-94,
+  :145-149): the index >= 16 test, the truncating conversion that folds
+  (-1, 0) into cell 0, and the 2*Size bound."""
 import numpy as np
 
 import oracle
@@ -81,3 +84,47 @@ def test_get_volume_at_truncates_toward_zero():
     assert oracle.get_volume_at(g, 0, 0, 0, 0) == 0
     # odd mip: any voxel of the 2^3 block
     assert oracle.get_volume_at(g, 0, 1, 1, 1) == 1
+
+
+def _translation(tx, ty, tz):
+    m = np.eye(4, dtype=np.float32)
+    m[:3, 3] = (tx, ty, tz)
+    return np.ascontiguousarray(m.T).reshape(16)  # column-major
+
+
+def test_voxelizer_known_answers():
+    """ShadowVoxSystem::OnUpdate's mapping (ShadowVoxSystem.cpp:145-149):
+    voxel (x,y,z) of index >= 16 goes to ivec3((o + x*dx + y*dy + z*dz) * 10),
+    dx = M[0] * 0.1 (fp32, truncating conversion), then SetVolumeAt
+    (:82-94: 0 <= x < 2*SizeX, bit (x&1)|(y&1)<<1|(z&1)<<2 of byte (x/2, y/2, z/2))."""
+    model = np.zeros((4, 4, 4), np.uint8)  # [z][y][x]
+    model[3, 2, 1] = 20   # -> fine (1,2,3): 0.1f*3*10 rounds to exactly 3
+    model[0, 0, 0] = 5    # index < 16 (glass): not a shadow caster
+    g = np.zeros((4, 4, 4), np.uint8)  # 8^3 fine voxels
+    oracle.voxelize_model(g, model, _translation(0, 0, 0), 1)
+    want = np.zeros_like(g)
+    want[1, 1, 0] = 1 << 5  # byte (0,1,1), bit 1 | 0 | 4
+    assert np.array_equal(g, want)
+
+    # truncation toward zero folds (-1, 0) into cell 0: x = 0 maps to (int)(-0.5) = 0
+    # and x = 1 to (int)(0.5) = 0, so both source voxels land in one cell
+    m2 = np.zeros((4, 4, 4), np.uint8)
+    m2[0, 0, 0] = 20
+    m2[0, 0, 1] = 20
+    g = np.zeros((4, 4, 4), np.uint8)
+    oracle.voxelize_model(g, m2, _translation(-0.05, 0, 0), 1)
+    want = np.zeros_like(g)
+    want[0, 0, 0] = 1
+    assert np.array_equal(g, want)
+
+    # SetVolumeAt's bound: x = 7 is set, x = 8 (= 2 * SizeX) is dropped
+    m3 = np.zeros((4, 4, 4), np.uint8)
+    m3[0, 0, 0] = 20
+    g = np.zeros((4, 4, 4), np.uint8)
+    oracle.voxelize_model(g, m3, _translation(0.7, 0, 0), 1)
+    want = np.zeros_like(g)
+    want[0, 0, 3] = 1 << 1
+    assert np.array_equal(g, want)
+    g = np.zeros((4, 4, 4), np.uint8)
+    oracle.voxelize_model(g, m3, _translation(0.8, 0, 0), 1)
+    assert not g.any()
