@@ -75,8 +75,9 @@ const char* vxl_status_string(vxl_status s);
  * lights, temporal accumulation, the depth-buffer and host-buffer occlusion
  * entries, the voxelizer's tables) reuse it from call to call: on one context,
  * such calls on different streams must not overlap (order them, or use one
- * context per stream). vxl_trace_occlusion and vxl_trace_rays keep no shared
- * state between calls and may overlap freely. */
+ * context per stream). vxl_trace_occlusion and vxl_trace_rays may overlap
+ * freely: each occlusion call takes its own work-queue counter from a ring of
+ * 4096 per context, so at most 4096 such calls may be in flight at once. */
 vxl_status vxl_ctx_create(int device, vxl_ctx** out);
 vxl_status vxl_ctx_destroy(vxl_ctx* ctx);
 /* number of kernels this library launched through ctx (diagnostics) */
