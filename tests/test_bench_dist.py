@@ -86,6 +86,11 @@ def test_reference_arm_runs_on_rank0_only():
     printed = [l for l in lines if l]
     assert len(printed) == 1  # rank 0 prints the one JSON line, rank 1 exits without work
     d = json.loads(printed[0].splitlines()[-1])
+    contract = {"impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"}
+    assert contract <= set(d), contract - set(d)
+    assert d["metric"].startswith("Grays/s") and d["unit"] == "Grays/s" and d["higher_is_better"] is True
+    assert d["config"]["workload"].startswith("plain-32^3-16x8") and d["steps"] == 1 and d["warmup"] == 0
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port"
     assert d["e2e"]["h2d_bytes_per_step"] == 0
