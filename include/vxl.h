@@ -76,8 +76,14 @@ const char* vxl_status_string(vxl_status s);
  * entries, the voxelizer's tables) reuse it from call to call: on one context,
  * such calls on different streams must not overlap (order them, or use one
  * context per stream). vxl_trace_occlusion and vxl_trace_rays may overlap
- * freely: each occlusion call takes its own work-queue counter from a ring of
- * 4096 per context, so at most 4096 such calls may be in flight at once. */
+ * freely: each uncaptured occlusion call takes its own work-queue counter
+ * from a ring of 4096 per context, so at most 4096 such calls may be in flight
+ * at once. An occlusion call made while its stream is capturing a CUDA graph
+ * keeps its counter for the life of that graph: it gets one of 4096 further
+ * counters that no other call of the context ever uses, so graph replays
+ * never share a counter with a direct call or another capture. A context
+ * accepts at most 4096 captured occlusion calls; the next one fails with
+ * VXL_ERR_NOT_SUPPORTED. Replays of one graph must not overlap. */
 vxl_status vxl_ctx_create(int device, vxl_ctx** out);
 vxl_status vxl_ctx_destroy(vxl_ctx* ctx);
 /* number of kernels this library launched through ctx (diagnostics) */
@@ -116,6 +122,8 @@ typedef struct vxl_grid_desc {
 } vxl_grid_desc;
 
 vxl_status vxl_grid_create(vxl_ctx* ctx, int nx, int ny, int nz, vxl_grid** out);
+/* frees the grid's device memory; allowed after its context was destroyed
+ * (no other call may use a grid whose context is gone) */
 vxl_status vxl_grid_destroy(vxl_grid* grid);
 vxl_status vxl_grid_describe(const vxl_grid* grid, vxl_grid_desc* out);
 /* zero every voxel */
@@ -406,7 +414,9 @@ vxl_status vxl_vox_destroyed(vxl_ctx* ctx, vxl_grid* grid, const vxl_model* mode
  *    VXL_ERR_OUT_OF_RANGE.
  *  - The first call on a device looks up the table's device address (once per
  *    device, with that device current); make that first call before any stream
- *    capture.
+ *    capture. The address is kept for the life of the process and belongs to
+ *    the device's primary context (the one the CUDA runtime uses): calls must
+ *    run in that context, and not after cudaDeviceReset on that device.
  *  - All calls share the one table: calls that overlap on the GPU (other
  *    streams, other host threads) race and must be serialised by the caller.
  *  - Same result as vxl_voxelize; returns when the update is complete. */

@@ -1,7 +1,8 @@
 """Recipe: compile the reference's own lighting-path sources on the host.
 
 TEST INFRASTRUCTURE ONLY (oracle pinning). Reads the VoxelEngine sources where
-they lie (default /root/reference, or $VXL_REFERENCE_DIR) and writes every
+they lie ($VXL_REFERENCE_DIR, else the tree `reference` beside this
+checkout) and writes every
 output into oracle/_ref/ (git-ignored):
 
 * Sources/Shaders/lib/Light.frag is compiled as C++ against the reference's
@@ -47,7 +48,10 @@ SO = os.path.join(OUT, "libvxl_ref.so")
 
 
 def reference_dir() -> str:
-    return os.environ.get("VXL_REFERENCE_DIR", "/root/reference")
+    """$VXL_REFERENCE_DIR, else a VoxelEngine tree named `reference` beside
+    this checkout."""
+    checkout = os.path.dirname(ORACLE)
+    return os.environ.get("VXL_REFERENCE_DIR", os.path.join(os.path.dirname(checkout), "reference"))
 
 
 def available() -> bool:

@@ -2,7 +2,8 @@
 this machine (oracle/ref/build_ref.py -> oracle/_ref/libvxl_ref.so).
 
 Run: python tests/golden/make_golden.py   (needs the VoxelEngine tree at
-/root/reference or $VXL_REFERENCE_DIR); `python tests/golden/make_golden.py
+$VXL_REFERENCE_DIR, or named `reference` beside this checkout);
+`python tests/golden/make_golden.py
 rayvox` writes only rayvox.npz. The fixtures let the oracle be checked
 against the reference where the reference tree is absent.
 """

@@ -1,4 +1,5 @@
-"""torch.autograd wrapper of the soft-opacity pass (vxl_trace_soft_fwd/_bwd).
+"""torch.autograd wrapper of the soft-opacity pass (vxl_trace_soft_fwd/_bwd),
+kept in the test harness: the library itself exposes only the C-ABI calls.
 
 ``SoftOcclusion.apply(soft, pos, nrm, params, ctx)`` returns the image
 [npix, 3]; its backward calls the hand-written adjoint kernel, which walks the
@@ -10,7 +11,7 @@ from __future__ import annotations
 
 import torch
 
-from . import trace_soft_bwd, trace_soft_fwd
+from voxelengine_gb300 import trace_soft_bwd, trace_soft_fwd
 
 
 class SoftOcclusion(torch.autograd.Function):

@@ -1,9 +1,16 @@
 """Batched tracing (vxl_batch_*: many scenes in one persistent launch,
 replayed from a CUDA graph) and tile-shape / queue-granularity knobs: every
-scene's buffers must equal a separate vxl_trace_occlusion of that scene, bit
-for bit, and the single-scene outputs must not depend on the tuning."""
+scene's buffers must equal the oracle's (oracle.occlusion on the scene's
+exported ShadowVox grid, Light.frag:29-81 driven as vxl_trace_occlusion
+drives it) and a separate vxl_trace_occlusion of that scene, bit for bit, and
+the single-scene outputs must not depend on the tuning."""
+import ctypes as C
+
 import numpy as np
 import pytest
+
+import oracle
+from tests.gpu_util import export_r8, same_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -24,6 +31,47 @@ def scenes(vxl, ctx):
             sc["params"] = vxl.make_params(cam_pos=sc["cam"], n_shadow=0, n_ao=12, ao_len=24.0, n_spec=2, seed=6)
         out.append(S.add_outputs(sc))
     return out
+
+
+@pytest.fixture(scope="module")
+def oracle_outs(scenes):
+    out = []
+    for sc in scenes:
+        op = oracle.Params()
+        C.memmove(C.byref(op), C.byref(sc["params"]), C.sizeof(op))  # same layout as vxl_trace_params
+        out.append(oracle.occlusion(export_r8(sc["grid"]), sc["pos"].cpu().numpy(), sc["nrm"].cpu().numpy(),
+                                    sc["rough"].cpu().numpy(), op))
+    return out
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+@pytest.mark.parametrize("tune", [None, (32, 4, 2, 2, 8, 2)])
+def test_batch_matches_oracle(vxl, ctx, scenes, oracle_outs, use_graph, tune):
+    """The batched kernel runs its own template instance (two step counters,
+    the bounds test at every step, every ray's t kept): its outputs are
+    checked against the oracle directly, not only against the single-scene
+    kernel."""
+    import torch
+
+    before = ctx.get_tuning()
+    try:
+        if tune:
+            ctx.set_tuning(*tune)
+        b = vxl.Batch(ctx, scenes, use_graph=use_graph)
+        for rep in range(2):
+            for sc in scenes:
+                for k in KEYS:
+                    sc[k].fill_(-1.0)
+            b.run()
+            torch.cuda.synchronize()
+            for i, (sc, w) in enumerate(zip(scenes, oracle_outs)):
+                for k in KEYS:
+                    ok = same_bits(sc[k].cpu().numpy(), w[k])
+                    assert ok.all(), "scene %d (%d^3) %s rep %d: %d of %d values differ" % (
+                        i, sc["n"], k, rep, int((~ok).sum()), ok.size)
+        b.close()
+    finally:
+        ctx.set_tuning(**before)
 
 
 def _single(vxl, ctx, sc):

@@ -108,7 +108,7 @@ def test_soft_autograd_mse(vxl, ctx):
     called directly with dL/dimage = 2 (I - I_t) / numel."""
     import torch
 
-    from voxelengine_gb300.soft import soft_occlusion
+    from tests.soft_autograd import soft_occlusion
 
     sc = _scene(vxl, ctx, n=64, W=64, H=64, n_ao=16)
     tgt = _scene(vxl, ctx, n=64, W=64, H=64, n_ao=16, albedo_seed=2)

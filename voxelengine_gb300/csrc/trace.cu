@@ -404,8 +404,11 @@ vxl_status launch_trace_rays(vxl_ctx* ctx, const vxl_grid* g, const float* rays,
 vxl_status launch_trace_occlusion(vxl_ctx* ctx, const vxl_grid* g, const vxl_gbuffer* gb, const vxl_trace_params* p,
                                   const vxl_outputs* out, cudaStream_t s) {
     if (gb->npix <= 0) return VXL_OK;
-    if (occl_pool_supported(g, p))
-        return launch_trace_occlusion_pool(ctx, g, gb, p, out, ctx_next_counter(ctx), ctx->tune, s);
+    if (occl_pool_supported(g, p)) {
+        unsigned long long* counter = nullptr;
+        VXL_TRY(ctx_take_counter(ctx, s, &counter));
+        return launch_trace_occlusion_pool(ctx, g, gb, p, out, counter, ctx->tune, s);
+    }
     GridView v = view_of(g);
     TraceConsts c;
     c.light = mk(p->light_dir[0], p->light_dir[1], p->light_dir[2]);

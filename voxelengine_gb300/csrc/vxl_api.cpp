@@ -76,7 +76,21 @@ static bool device_view(const vxl_ctx* ctx, const void* h, void** d) {
     return true;
 }
 
-unsigned long long* ctx_next_counter(vxl_ctx* ctx) { return ctx->d_counters + (ctx->counter_next++ % kCounterRing); }
+vxl_status ctx_take_counter(vxl_ctx* ctx, cudaStream_t s, unsigned long long** out) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    VXL_TRY_CUDA(cudaStreamIsCapturing(s, &cs));
+    if (cs == cudaStreamCaptureStatusNone) {
+        *out = ctx->d_counters + (ctx->counter_next++ % kCounterRing);
+        return VXL_OK;
+    }
+    // a captured launch replays with this counter for as long as its graph
+    // lives: give it a slot that no other launch of this context ever gets
+    if (ctx->capture_next >= kCaptureCounters)
+        return fail(VXL_ERR_NOT_SUPPORTED, "trace_occlusion: more than %u captured occlusion calls on one context",
+                    kCaptureCounters);
+    *out = ctx->d_counters + kCounterRing + ctx->capture_next++;
+    return VXL_OK;
+}
 
 // glm::translate(m, v): Result[3] = m[0]*v[0] + m[1]*v[1] + m[2]*v[2] + m[3]
 static void translate(const float* m, const float* v, float* out) {
@@ -215,8 +229,9 @@ vxl_status vxl_ctx_create(int device, vxl_ctx** out) {
     c->device = device;
     e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device);
-    if (e == cudaSuccess) e = cudaMalloc(&c->d_counters, kCounterRing * sizeof(unsigned long long));
-    if (e == cudaSuccess) e = cudaMemset(c->d_counters, 0, kCounterRing * sizeof(unsigned long long));
+    const size_t counter_bytes = (size_t)(kCounterRing + kCaptureCounters) * sizeof(unsigned long long);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_counters, counter_bytes);
+    if (e == cudaSuccess) e = cudaMemset(c->d_counters, 0, counter_bytes);
     if (e != cudaSuccess) {
         if (c->d_counters) cudaFree(c->d_counters);
         delete c;
@@ -311,6 +326,7 @@ vxl_status vxl_grid_create(vxl_ctx* ctx, int nx, int ny, int nz, vxl_grid** out)
     vxl_grid* g = new (std::nothrow) vxl_grid();
     if (!g) return fail(VXL_ERR_OOM, "grid_create: host allocation");
     g->ctx = ctx;
+    g->device = ctx->device;
     g->nx = nx;
     g->ny = ny;
     g->nz = nz;
@@ -338,7 +354,7 @@ vxl_status vxl_grid_create(vxl_ctx* ctx, int nx, int ny, int nz, vxl_grid** out)
 
 vxl_status vxl_grid_destroy(vxl_grid* g) {
     if (!g) return VXL_OK;
-    cudaSetDevice(g->ctx->device);
+    cudaSetDevice(g->device);  // the context may already be gone
     cudaFree(g->words);
     cudaFree(g->tmask);
     delete g;
@@ -544,7 +560,9 @@ vxl_status vxl_trace_occlusion_host(vxl_ctx* ctx, const vxl_grid* g, const float
         vxl_gbuffer gb{d_pos + 3 * p0, d_nrm + 3 * p0, h_rough ? d_rough + p0 : nullptr, n, 0, 0};
         vxl_outputs o{hs[0] ? outs[0] + p0 : nullptr, hs[1] ? outs[1] + p0 : nullptr, hs[2] ? outs[2] + p0 : nullptr,
                       hs[3] ? outs[3] + p0 : nullptr, hs[4] ? outs[4] + p0 : nullptr, nullptr};
-        VXL_TRY(launch_trace_occlusion_pool(ctx, g, &gb, p, &o, ctx_next_counter(ctx), ctx->tune, cs,
+        unsigned long long* counter = nullptr;
+        VXL_TRY(ctx_take_counter(ctx, cs, &counter));
+        VXL_TRY(launch_trace_occlusion_pool(ctx, g, &gb, p, &o, counter, ctx->tune, cs,
                                             (uint32_t)p0));
         for (int k = 0; k < 5; k++)
             if (hs[k])

@@ -18,11 +18,14 @@ struct vxl_ctx {
     size_t d_scratch_bytes;
     void* d_stage;
     size_t d_stage_bytes;
-    // ring of work-queue counters for the persistent kernels: each launch
-    // takes the next one, so launches in flight on different streams never
-    // share a counter
+    // work-queue counters of the persistent kernels. Uncaptured launches take
+    // the next slot of a ring of kCounterRing, so launches in flight on
+    // different streams never share a counter. A launch recorded into a CUDA
+    // graph keeps its counter for the graph's life: it takes one of
+    // kCaptureCounters further slots, each handed out once per context.
     unsigned long long* d_counters;
     uint32_t counter_next;
+    uint32_t capture_next;
     vxl_tuning tune;  // occlusion kernel launch shape (vxl_ctx_set_tuning)
     // copy / compute pipeline of the host-buffer entry point (created on first use)
     cudaStream_t pipe[2];
@@ -48,9 +51,11 @@ struct vxl_ctx {
     size_t lpairs_bytes;
 };
 constexpr uint32_t kCounterRing = 4096;
+constexpr uint32_t kCaptureCounters = 4096;
 
 struct vxl_grid {
     vxl_ctx* ctx;
+    int device;      // ctx->device, kept so that the grid can be destroyed after its context
     int nx, ny, nz;
     int bx, by, bz;  // 4^3 bricks per axis, one padding brick included
     int tx, ty, tz;  // 8^3 tiles per axis (tile map)
@@ -133,7 +138,8 @@ vxl_status launch_trace_occlusion_pool(vxl_ctx* ctx, const vxl_grid* g, const vx
                                        const vxl_trace_params* p, const vxl_outputs* out,
                                        unsigned long long* d_counter, const vxl_tuning& tune, cudaStream_t s,
                                        uint32_t pix_base = 0);
-unsigned long long* ctx_next_counter(vxl_ctx* ctx);
+// the work-queue counter for one persistent launch on stream s (see d_counters)
+vxl_status ctx_take_counter(vxl_ctx* ctx, cudaStream_t s, unsigned long long** out);
 // batched occlusion: scene table built on the host, uploaded once, one launch
 size_t batch_desc_bytes();
 vxl_status batch_build_table(const vxl_batch_item* items, int n, const vxl_tuning& tune, void* h_table, int* max_r,
