@@ -47,7 +47,7 @@
 extern "C" {
 #endif
 
-#define VXL_ABI_VERSION 1
+#define VXL_ABI_VERSION 2
 
 typedef enum vxl_status {
     VXL_OK = 0,
@@ -110,7 +110,19 @@ vxl_status vxl_ctx_get_tuning(const vxl_ctx* ctx, vxl_tuning* out);
  * 4x4x4 bricks, one uint64 each (bit (x&3) + 4*(y&3) + 16*(z&3)), bricks in
  * x-fastest order, plus one zero brick of padding on the + side of every
  * axis; and a tile map with 1 bit per 8^3 tile (2x2x2 bricks), x-fastest.
- * nx, ny, nz must be even and in [2, 32768]. */
+ * nx, ny, nz must be even and in [2, 32768].
+ *
+ * Derived from the words, for the occlusion traversal: the trace layout. The
+ * same 4^3 bricks, with every cell shifted by +4 on each axis (cell x is at
+ * x + 4), 2^trace_lbx bricks per x row and 2^trace_lby per y column (powers
+ * of two, padding included) and trace_bz z slabs, brick (i, j, k) at word
+ * i + (j << trace_lbx) + (k << (trace_lbx + trace_lby)). A cell holds the
+ * grid's voxel inside [0, n), 0 in the DDA's two extra cells n and n+1
+ * (Light.frag:53 tests up to 2S+1 inclusive) and 1 on the border just
+ * outside those bounds (a coordinate equal to -1 or n+2). The traversal then
+ * needs no bounds test: the first cell outside the bounds reads as set, and
+ * is reported as the bounds exit. Present when every bit address fits in 32
+ * bits (trace_words != NULL); rebuilt with the tile map. */
 typedef struct vxl_grid_desc {
     int32_t nx, ny, nz;        /* fine dimensions */
     int32_t bx, by, bz;        /* 4^3 bricks per axis, padding included */
@@ -119,6 +131,10 @@ typedef struct vxl_grid_desc {
     size_t words_bytes;
     uint32_t* tile_mask;       /* device: 1 bit per tile, "tile has any voxel set" */
     size_t tile_mask_bytes;
+    uint64_t* trace_words;     /* device: the trace layout, or NULL */
+    size_t trace_words_bytes;
+    int32_t trace_lbx, trace_lby, trace_bz;
+    int32_t pad;
 } vxl_grid_desc;
 
 vxl_status vxl_grid_create(vxl_ctx* ctx, int nx, int ny, int nz, vxl_grid** out);
@@ -128,8 +144,10 @@ vxl_status vxl_grid_destroy(vxl_grid* grid);
 vxl_status vxl_grid_describe(const vxl_grid* grid, vxl_grid_desc* out);
 /* zero every voxel */
 vxl_status vxl_grid_clear(vxl_grid* grid, void* stream);
-/* rebuild the tile occupancy map after the words changed (the trace entry
- * points read it); vxl_voxelize and the imports rebuild it themselves */
+/* rebuild the tile occupancy map and the trace layout after the words
+ * changed (the trace entry points read them); every call of this library
+ * that writes a grid (vxl_voxelize, vxl_voxelize_noalloc, the imports, the
+ * scene generators, vxl_grid_clear) rebuilds them itself */
 vxl_status vxl_grid_build_bricks(vxl_grid* grid, void* stream);
 /* Reference layout in/out: device bytes [nz/2][ny/2][nx/2], byte x+y*sx+z*sx*sy,
  * bit (x&1)|(y&1)<<1|(z&1)<<2 (ShadowVoxSystem.cpp:82-94, Light.frag:14-20). */

@@ -44,7 +44,7 @@ def test_binding_declares_every_argument_list(V):
 
 def test_abi_version_and_status_strings(V):
     L = V.lib()
-    assert L.vxl_abi_version() == 1
+    assert L.vxl_abi_version() == 2
     assert L.vxl_status_string(0) == b"VXL_OK"
     assert L.vxl_status_string(5) == b"VXL_ERR_OUT_OF_RANGE"
 

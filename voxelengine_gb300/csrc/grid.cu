@@ -91,6 +91,33 @@ __global__ void k_tile_mask(GridView g, uint32_t* mask, int by_, int bz_, uint32
     if ((threadIdx.x & 31) == 0) mask[t >> 5] = m;
 }
 
+// Trace layout word i: the grid's brick at (bricks shifted by one on every
+// axis) plus the border cells it holds.
+__global__ void k_trace_layout(GridView g, TraceLayout t, uint32_t nwords) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nwords) return;
+    const int qx = (int)(i & ((1u << t.lbx) - 1u));
+    const int qy = (int)((i >> t.lbx) & ((1u << t.lby) - 1u));
+    const int qz = (int)(i >> (t.lbx + t.lby));
+    uint64_t w = 0;
+    const int cx = qx - 1, cy = qy - 1, cz = qz - 1;  // the grid's brick
+    const int gby = (int)(g.bxy / (uint32_t)g.bx), gbz = ((g.nz + 3) >> 2) + 1;
+    if (cx >= 0 && cy >= 0 && cz >= 0 && cx < g.bx && cy < gby && cz < gbz)
+        w = g.words[(uint32_t)cx + (uint32_t)cy * (uint32_t)g.bx + (uint32_t)cz * g.bxy];
+    // border: shifted coordinates 3 (cell -1) and n+6 (cell n+2)
+    const int ex = t.nx + 6, ey = t.ny + 6, ez = t.nz + 6;
+    const bool touches = qx == 0 || qx == (ex >> 2) || qy == 0 || qy == (ey >> 2) || qz == 0 || qz == (ez >> 2);
+    if (touches) {
+        for (int b = 0; b < 64; b++) {
+            const int x = 4 * qx + (b & 3), y = 4 * qy + ((b >> 2) & 3), z = 4 * qz + (b >> 4);
+            const bool inbox = x >= 3 && x <= ex && y >= 3 && y <= ey && z >= 3 && z <= ez;
+            const bool face = x == 3 || x == ex || y == 3 || y == ey || z == 3 || z == ez;
+            if (inbox && face) w |= 1ull << b;
+        }
+    }
+    t.words[i] = w;
+}
+
 __global__ void k_count(const uint64_t* __restrict__ words, size_t n, unsigned long long* out) {
     unsigned long long c = 0;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -341,12 +368,43 @@ vxl_status launch_grid_import_palette(vxl_grid* g, const uint8_t* pal, int opaqu
     return launch_build_tile_mask(g, s);
 }
 
+void trace_layout_dims(vxl_grid* g) {
+    auto lg = [](int v) {
+        int l = 0;
+        while ((1 << l) < v) l++;
+        return l;
+    };
+    // bricks covering shifted cells [3, n+6] (cells -1 .. n+2)
+    const int cx = ((g->nx + 6) >> 2) + 1, cy = ((g->ny + 6) >> 2) + 1, cz = ((g->nz + 6) >> 2) + 1;
+    g->tl_lbx = lg(cx);
+    g->tl_lby = lg(cy);
+    g->tl_bz = cz;
+    const int sh = 6 + g->tl_lbx + g->tl_lby;
+    // every bit address must fit in 32 bits
+    if (sh >= 32 || ((unsigned long long)cz << sh) > (1ull << 32)) {
+        g->tl_nwords = 0;
+        return;
+    }
+    g->tl_nwords = (size_t)cz << (g->tl_lbx + g->tl_lby);
+}
+
+cudaError_t launch_trace_layout_view(const GridView& v, const TraceLayout& t, cudaStream_t s) {
+    const size_t n = (size_t)t.bz << (t.lbx + t.lby);
+    k_trace_layout<<<blocks_for(n, 256), 256, 0, s>>>(v, t, (uint32_t)n);
+    return cudaGetLastError();
+}
+
 vxl_status launch_build_tile_mask(vxl_grid* g, cudaStream_t s) {
     uint32_t ntiles = (uint32_t)((size_t)g->tx * g->ty * g->tz);
     k_tile_mask<<<blocks_for(g->nmask * 32, 256), 256, 0, s>>>(view_of(g), g->tmask, g->by, g->bz, ntiles,
                                                              (uint32_t)g->nmask);
     g->ctx->launches++;
     VXL_TRY_CUDA(cudaGetLastError());
+    if (g->tl_words) {
+        TraceLayout t{g->tl_words, g->tl_lbx, g->tl_lby, g->tl_bz, g->nx, g->ny, g->nz};
+        VXL_TRY_CUDA(launch_trace_layout_view(view_of(g), t, s));
+        g->ctx->launches++;
+    }
     return VXL_OK;
 }
 

@@ -101,6 +101,7 @@ __global__ void __launch_bounds__(256) k_voxelize_na(GridView g, unsigned long l
 
 cudaError_t launch_tile_mask_view(const GridView& v, uint32_t* mask, int by, int bz, int tx, int ty, int tz,
                                   cudaStream_t s);
+cudaError_t launch_trace_layout_view(const GridView& v, const TraceLayout& t, cudaStream_t s);
 
 }  // namespace vxl
 
@@ -113,6 +114,16 @@ extern "C" vxl_status vxl_voxelize_noalloc(const vxl_grid_desc* gd, const vxl_mo
         gd->bx != (gd->nx + 3) / 4 + 1 || gd->by != (gd->ny + 3) / 4 + 1 || gd->bz != (gd->nz + 3) / 4 + 1 ||
         gd->tx != (gd->bx + 1) / 2 || gd->ty != (gd->by + 1) / 2 || gd->tz != (gd->bz + 1) / 2)
         return fail(VXL_ERR_INVALID_ARG, "voxelize_noalloc: grid descriptor does not describe a vxl grid layout");
+    if (gd->trace_words) {
+        vxl_grid d{};
+        d.nx = gd->nx;
+        d.ny = gd->ny;
+        d.nz = gd->nz;
+        trace_layout_dims(&d);
+        if (!d.tl_nwords || gd->trace_lbx != d.tl_lbx || gd->trace_lby != d.tl_lby || gd->trace_bz != d.tl_bz ||
+            gd->trace_words_bytes < d.tl_nwords * sizeof(uint64_t))
+            return fail(VXL_ERR_INVALID_ARG, "voxelize_noalloc: grid descriptor's trace layout does not match its dims");
+    }
     if (n < 0 || (n > 0 && !instances)) return fail(VXL_ERR_INVALID_ARG, "voxelize_noalloc: bad instances");
     if (nmodels < 0 || (nmodels > 0 && !models)) return fail(VXL_ERR_INVALID_ARG, "voxelize_noalloc: bad models");
     if (n > VXL_NOALLOC_MAX_INSTANCES)
@@ -172,6 +183,10 @@ extern "C" vxl_status vxl_voxelize_noalloc(const vxl_grid_desc* gd, const vxl_mo
         i = j;
     }
     VXL_TRY_CUDA(launch_tile_mask_view(v, gd->tile_mask, gd->by, gd->bz, gd->tx, gd->ty, gd->tz, s));
+    if (gd->trace_words) {
+        const TraceLayout t{gd->trace_words, gd->trace_lbx, gd->trace_lby, gd->trace_bz, gd->nx, gd->ny, gd->nz};
+        VXL_TRY_CUDA(launch_trace_layout_view(v, t, s));
+    }
     // the copies read the caller's host arrays: finish before returning them
     VXL_TRY_CUDA(cudaStreamSynchronize(s));
     return VXL_OK;

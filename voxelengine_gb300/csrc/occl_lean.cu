@@ -1,0 +1,377 @@
+// occl_lean.cu — the DDA-mode occlusion pass (vxl_trace_occlusion without
+// per-ray records) on the grid's trace layout.
+//
+// Same ray generator, dispatch order, warp pools and per-pixel fold as the
+// kernels of occlusion.cu, so the outputs are bit-identical; what changes is
+// the inner loop of raycastShadowVolume (Sources/Shaders/lib/Light.frag:50-75):
+//  - The cell is held as a bit address A = ax + ay + az in the trace layout,
+//    one term per axis (vxl_device.cuh, AxisCode). A step along an axis is an
+//    add and a mask on that axis's term; the fetch is one 32-bit load and a
+//    funnel shift.
+//  - No bounds test: the trace layout's border cells (one cell outside the
+//    DDA's inclusive bounds) read as set. A set cell is a hit unless it lies
+//    outside [0, n+1] on some axis, which is the reference's bounds exit at
+//    that same iteration (Light.frag:53).
+//  - The `totalt < maxt` test of the loop (Light.frag:75) is taken out of the
+//    loop body. Without exact ties, totalt of an iteration is the smallest
+//    t_max component, which never decreases from one iteration to the next,
+//    so the first iteration whose totalt reaches maxt is found later: at a set
+//    cell (the previous iteration's totalt) and at the end of a batch of
+//    KSTEP iterations. An iteration with an exact tie (totalt = the sum of the
+//    tied components, which can exceed later ones) is tested at once. Steps a
+//    lane takes past its ray's end only touch cells inside the border.
+//  - The 256-iteration cap (Light.frag:75) is tested per batch: a batch that
+//    might reach it runs the iterations with the cap and maxt tests in place.
+#include "occl_common.cuh"
+
+namespace vxl {
+
+struct LeanGrid {
+    const uint32_t* __restrict__ w;  // trace layout, as 32-bit halves of the brick words
+    uint32_t field[3];                // bits of A owned by each axis
+    uint32_t keep[3];                 // mask after a step (clears the axis's gap)
+    uint32_t inc[3];                  // +1 step increment; a -1 step adds -unit
+    uint32_t unit[3];
+    uint32_t lo[3], span[3];          // axis term of shifted coordinate 4 and the span up to n+5
+    int hs[3];                        // shift of each axis's brick index
+};
+
+struct LeanScene {
+    SceneDesc S;
+    LeanGrid L;
+};
+
+LeanGrid lean_grid_of(const vxl_grid* g) {
+    LeanGrid L;
+    L.w = reinterpret_cast<const uint32_t*>(g->tl_words);
+    const int n[3] = {g->nx, g->ny, g->nz};
+    for (int a = 0; a < 3; a++) {
+        const AxisCode c = axis_code(a, g->tl_lbx, g->tl_lby);
+        L.field[a] = c.field;
+        L.keep[a] = c.keep;
+        L.inc[a] = c.inc;
+        L.unit[a] = c.unit;
+        L.hs[a] = c.hi_shift;
+        // interior cells 0 .. n+1 are shifted cells 4 .. n+5
+        L.lo[a] = axis_term(c, 4);
+        L.span[a] = axis_term(c, n[a] + 5) - L.lo[a];
+    }
+    return L;
+}
+
+// One iteration of Light.frag:50-75 on the trace layout. Returns 0 while the
+// ray goes on, 1 for a hit (t in *ht), 2 when the ray ends without one.
+// `tot` is the previous iteration's totalt (-inf before the first).
+__device__ __forceinline__ int lean_step(const LeanGrid& L, uint32_t& ax, uint32_t& ay, uint32_t& az, float& tx,
+                                         float& ty, float& tz, float tdx, float tdy, float tdz, uint32_t kx,
+                                         uint32_t ky, uint32_t kz, float maxt, float& tot, float* ht) {
+    const uint32_t a = ax + ay + az;  // the terms' bit fields do not overlap
+    const uint32_t w = __ldg(L.w + (a >> 5));
+    const float m = fminf(fminf(tx, ty), tz);
+    // select = step(t.xyz, t.zxy) * step(t.xyz, t.yzx): the components equal to the minimum
+    const bool bx = tx == m, by = ty == m, bz = tz == m;
+    const bool tie = (bx && (by || bz)) || (by && bz);
+    if (__funnelshift_r(w, w, a) & 1u) {
+        if (!(tot < maxt)) return 2;  // the loop had ended before this iteration
+        // a border cell: the bounds test of this iteration fails (Light.frag:53)
+        if (ax - L.lo[0] > L.span[0] || ay - L.lo[1] > L.span[1] || az - L.lo[2] > L.span[2]) return 2;
+        // dot(t_max, select); +0.0f turns a -0 minimum into the +0 the dot product gives
+        float best = m + 0.0f;
+        if (tie) {
+            best = (bx ? tx : 0.0f) + (by ? ty : 0.0f);
+            best = best + (bz ? tz : 0.0f);
+        }
+        *ht = best;
+        return 1;
+    }
+    float best = m;
+    if (tie) {
+        best = (bx ? tx : 0.0f) + (by ? ty : 0.0f);
+        best = best + (bz ? tz : 0.0f);
+        if (!(best < maxt)) return 2;
+    }
+    if (bx) {
+        ax = (ax + kx) & L.keep[0];
+        tx = tx + tdx;
+    }
+    if (by) {
+        ay = (ay + ky) & L.keep[1];
+        ty = ty + tdy;
+    }
+    if (bz) {
+        az = (az + kz) & L.keep[2];
+        tz = tz + tdz;
+    }
+    tot = best;
+    return 0;
+}
+
+#ifndef VXL_LEAN_MIN_BLOCKS
+#define VXL_LEAN_MIN_BLOCKS 8
+#endif
+
+template <int TP, int KSTEP>
+__global__ void __launch_bounds__(128, VXL_LEAN_MIN_BLOCKS) k_occl_lean(const LeanScene P,
+                                                                        unsigned long long* __restrict__ counter,
+                                                                        int grab) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const SceneDesc& S = P.S;
+    const LeanGrid& L = P.L;
+    const TraceConstsP& c = S.c;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int R = c.R;
+    unsigned char* wbase = smem + warp * pool_bytes(TP, R);
+    PSlot* slots = reinterpret_cast<PSlot*>(wbase);
+    float* res_t = reinterpret_cast<float*>(wbase + (size_t)TP * R * sizeof(PSlot));
+    uint32_t* res_hit = reinterpret_cast<uint32_t*>(wbase + (size_t)TP * R * (sizeof(PSlot) + sizeof(float)));
+    const unsigned ux = S.g.ux, uy = S.g.uy, uz = S.g.uz;
+    constexpr int LPP = 32 / TP;  // lanes per pixel during generation
+
+    for (;;) {
+        int64_t t0 = 0;
+        if (lane == 0) t0 = (int64_t)atomicAdd(counter, (unsigned long long)grab);
+        t0 = __shfl_sync(0xffffffffu, t0, 0);
+        if (t0 >= S.ntiles) break;
+        for (int gi = 0; gi < grab && t0 + gi < S.ntiles; gi++) {
+            const int64_t tile = t0 + gi;
+            // ------------------------------------------------ A: generation
+            const int p = lane % TP;
+            int64_t gpix;
+            const bool inimg = tile_pixel<TP>(S, tile, p, &gpix);
+            f3 Pp = mk(0.0f, 0.0f, 0.0f), N = mk(0.0f, 0.0f, 0.0f);
+            float ro = c.default_rough;
+            if (inimg) {
+                Pp = ld3(S.pos + 3 * gpix);
+                N = ld3(S.nrm + 3 * gpix);
+                if (S.rough) ro = S.rough[gpix];
+            }
+            const bool sky = !inimg || (N.x == 0.0f && N.y == 0.0f && N.z == 0.0f);
+            const f3 O = add(Pp, mul(N, c.bias));
+            f3 T, B;
+            tangent_frame(N, &T, &B);
+            for (int k = lane; k < R; k += 32) res_hit[k] = 0u;
+            int live = 0;
+            const int rounds = (R + LPP - 1) / LPP;
+            for (int j = 0; j < rounds; j++) {
+                const int kk = j * LPP + lane / TP;
+                const int k = !c.spec_first ? kk : (kk < c.n_spec ? c.n_shadow + c.n_ao + kk : kk - c.n_spec);
+                bool is_live = false;
+                PSlot sl;
+                if (kk < R && !sky) {
+                    const f3 d = gen_dir(c, k, (uint32_t)gpix + S.pix_base, Pp, N, T, B, ro);
+                    const float maxt = kind_maxt(c, k);
+                    const int meta = (p << 4) | (k << 9);
+                    if (!ray_domain_ok(O, d)) {
+                        // no traversal: a miss
+                    } else if (!dir_fast_ok(d)) {
+                        is_live = true;
+                        sl.c01 = 0;
+                        sl.c2m = (meta | kMetaLit) << 16;
+                        sl.a0 = O.x; sl.a1 = O.y; sl.a2 = O.z;
+                        sl.b0 = d.x; sl.b1 = d.y; sl.b2 = d.z;
+                    } else {
+                        DState s;
+                        dda_init(s, O, d, maxt);
+                        // an origin cell outside the bounds ends the ray at the first test (Light.frag:53)
+                        if ((unsigned)s.cx <= ux && (unsigned)s.cy <= uy && (unsigned)s.cz <= uz) {
+                            is_live = true;
+                            const int sg = (s.sx < 0 ? 1 : 0) | (s.sy < 0 ? 2 : 0) | (s.sz < 0 ? 4 : 0);
+                            const uint32_t xs = (uint32_t)(s.cx + 4), ys = (uint32_t)(s.cy + 4), zs = (uint32_t)(s.cz + 4);
+                            sl.c01 = (int)((xs & 3u) | ((xs >> 2) << L.hs[0]) | ((ys & 3u) << 2) | ((ys >> 2) << L.hs[1]) |
+                                           ((zs & 3u) << 4) | ((zs >> 2) << L.hs[2]));
+                            sl.c2m = (meta | sg) << 16;
+                            sl.a0 = s.tx; sl.a1 = s.ty; sl.a2 = s.tz;
+                            sl.b0 = s.tdx; sl.b1 = s.tdy; sl.b2 = s.tdz;
+                        }
+                    }
+                }
+                const unsigned lv = __ballot_sync(0xffffffffu, is_live);
+                if (is_live) slots[live + __popc(lv & lanes_below())] = sl;
+                live += __popc(lv);
+            }
+            __syncwarp();
+
+            // ------------------------------------------------- B: traversal
+            int base = 0;
+            bool busy = false, retired = false;
+            uint32_t ax = 0, ay = 0, az = 0, kx = 0, ky = 0, kz = 0;
+            float tx = 0.0f, ty = 0.0f, tz = 0.0f, tdx = 0.0f, tdy = 0.0f, tdz = 0.0f, maxt = 0.0f, tot = 0.0f;
+            int n = 0, meta = 0;
+            for (;;) {
+                const bool need = !busy && !retired;
+                const unsigned nm = __ballot_sync(0xffffffffu, need);
+                if (nm) {
+                    if (need) {
+                        const int at = base + __popc(nm & lanes_below());
+                        if (at < live) {
+                            const PSlot sl = slots[at];
+                            meta = (unsigned)sl.c2m >> 16;
+                            const int k = (meta >> 9) & 31;
+                            maxt = kind_maxt(c, k);
+                            if (meta & kMetaLit) {
+                                const Hit h = dda_literal(S.g, mk(sl.a0, sl.a1, sl.a2), mk(sl.b0, sl.b1, sl.b2), maxt);
+                                if (h.flags & VXL_RF_HIT) {
+                                    const int pp = (meta >> 4) & 31;
+                                    res_t[k * TP + pp] = h.t;
+                                    atomicOr(&res_hit[k], 1u << pp);
+                                }
+                            } else {
+                                busy = true;
+                                const uint32_t A = (uint32_t)sl.c01;
+                                ax = A & L.field[0];
+                                ay = A & L.field[1];
+                                az = A & L.field[2];
+                                kx = (meta & 1) ? 0u - L.unit[0] : L.inc[0];
+                                ky = (meta & 2) ? 0u - L.unit[1] : L.inc[1];
+                                kz = (meta & 4) ? 0u - L.unit[2] : L.inc[2];
+                                tx = sl.a0; ty = sl.a1; tz = sl.a2;
+                                tdx = sl.b0; tdy = sl.b1; tdz = sl.b2;
+                                tot = -INFINITY;
+                                n = 0;
+                            }
+                        } else {
+                            retired = true;
+                        }
+                    }
+                    base += __popc(nm);
+                }
+                if (!__any_sync(0xffffffffu, busy) && base >= live) break;
+                if (busy) {
+                    int res = 0;
+                    float ht = 0.0f;
+                    if (__all_sync(__activemask(), n + KSTEP <= 256)) {
+#pragma unroll
+                        for (int it = 0; it < KSTEP; it++) {
+                            res = lean_step(L, ax, ay, az, tx, ty, tz, tdx, tdy, tdz, kx, ky, kz, maxt, tot, &ht);
+                            if (res) break;
+                        }
+                        if (!res) {
+                            n += KSTEP;
+                            if (!(tot < maxt)) res = 2;
+                        }
+                    } else {
+                        // the batch may reach the 256-iteration cap: test it, and maxt, at every iteration
+                        for (int it = 0; it < KSTEP; it++) {
+                            if (n >= 256) {
+                                res = 2;
+                                break;
+                            }
+                            res = lean_step(L, ax, ay, az, tx, ty, tz, tdx, tdy, tdz, kx, ky, kz, maxt, tot, &ht);
+                            if (res) break;
+                            n++;
+                            if (!(tot < maxt) || n >= 256) {
+                                res = 2;
+                                break;
+                            }
+                        }
+                    }
+                    if (res) {
+                        if (res == 1) {
+                            const int k = (meta >> 9) & 31, pp = (meta >> 4) & 31;
+                            res_t[k * TP + pp] = ht;
+                            atomicOr(&res_hit[k], 1u << pp);
+                        }
+                        busy = false;
+                    }
+                }
+            }
+            __syncwarp();
+
+            // ------------------------------------------------------ C: fold
+            if (lane < TP && inimg) {
+                float sh = 1.0f, ao = 1.0f, vis = 1.0f, sp = 1.0f, st = c.spec_len;
+                if (!sky) {
+                    int k = 0;
+                    if (c.n_shadow > 0) {
+                        sh = ((res_hit[0] >> p) & 1u) ? 0.0f : 1.0f;
+                        k = 1;
+                    }
+                    float acc = 0.0f, v = 0.0f;
+                    for (int j = 0; j < c.n_ao; j++, k++) {
+                        const bool hit = (res_hit[k] >> p) & 1u;
+                        const float t = res_t[k * TP + p];
+                        float tt = hit ? (t < c.ao_len ? t : c.ao_len) : c.ao_len;
+                        float q = tt / c.ao_len;
+                        acc += q * q;
+                        v += hit ? 0.0f : 1.0f;
+                    }
+                    if (c.n_ao > 0) {
+                        ao = acc / (float)c.n_ao;
+                        vis = v / (float)c.n_ao;
+                    }
+                    if (c.n_spec > 0) {
+                        float spa = 0.0f, sta = 0.0f;
+                        for (int j = 0; j < c.n_spec; j++, k++) {
+                            const bool hit = (res_hit[k] >> p) & 1u;
+                            spa += hit ? 0.0f : 1.0f;
+                            sta += hit ? res_t[k * TP + p] : c.spec_len;
+                        }
+                        sp = spa / (float)c.n_spec;
+                        st = sta / (float)c.n_spec;
+                    }
+                }
+                if (S.o_shadow) S.o_shadow[gpix] = sh;
+                if (S.o_ao) S.o_ao[gpix] = ao;
+                if (S.o_vis) S.o_vis[gpix] = vis;
+                if (S.o_spec) S.o_spec[gpix] = sp;
+                if (S.o_spec_t) S.o_spec_t[gpix] = st;
+            }
+            __syncwarp();
+        }
+    }
+}
+
+template <int TP, int KSTEP>
+static vxl_status launch_lean_t(vxl_ctx* ctx, const LeanScene& P, unsigned long long* counter, int grab,
+                                cudaStream_t s) {
+    const size_t smem = pool_bytes(TP, P.S.c.R) * 4;
+    auto kern = k_occl_lean<TP, KSTEP>;
+    VXL_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    VXL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem));
+    if (per_sm < 1) return fail(VXL_ERR_NOT_SUPPORTED, "occlusion pool: %zu bytes of shared memory per block", smem);
+    int64_t blocks = (int64_t)ctx->sm_count * per_sm;
+    const int64_t warps_needed = (P.S.ntiles + grab - 1) / grab;
+    if (blocks * 4 > warps_needed) blocks = (warps_needed + 3) / 4;
+    kern<<<(unsigned)blocks, 128, smem, s>>>(P, counter, grab);
+    ctx->launches++;
+    VXL_TRY_CUDA(cudaGetLastError());
+    return VXL_OK;
+}
+
+template <int TP>
+static vxl_status launch_lean_k(vxl_ctx* ctx, const LeanScene& P, unsigned long long* counter, const vxl_tuning& t,
+                                cudaStream_t s) {
+    switch (t.kstep) {
+        case 4: return launch_lean_t<TP, 4>(ctx, P, counter, t.grab, s);
+        case 16: return launch_lean_t<TP, 16>(ctx, P, counter, t.grab, s);
+        default: return launch_lean_t<TP, 8>(ctx, P, counter, t.grab, s);
+    }
+}
+
+bool occl_lean_supported(const vxl_grid* g, const vxl_outputs* out, const vxl_tuning& tune) {
+    return g->tl_words != nullptr && !out->records && tune.leap != 1;
+}
+
+vxl_status launch_trace_occlusion_lean(vxl_ctx* ctx, const vxl_grid* g, const vxl_gbuffer* gb,
+                                       const vxl_trace_params* p, const vxl_outputs* out,
+                                       unsigned long long* d_counter, const vxl_tuning& tune, cudaStream_t s,
+                                       uint32_t pix_base) {
+    const int R = p->n_shadow + p->n_ao + p->n_spec;
+    vxl_tuning t = tune;
+    // many rays per pixel: 8-pixel tiles keep the pool's shared memory within 8 blocks per SM
+    if (t.tile_px == 16 && (pool_bytes(16, R) * 4 + 1024) * VXL_LEAN_MIN_BLOCKS > (size_t)ctx->smem_per_sm) {
+        t.tile_px = 8;
+        t.tile_w = 8;
+    }
+    LeanScene P;
+    P.S = scene_of(g, gb, p, out, t);
+    P.S.pix_base = pix_base;
+    P.L = lean_grid_of(g);
+    VXL_TRY_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s));
+    if (t.tile_px == 8) return launch_lean_k<8>(ctx, P, d_counter, t, s);
+    if (t.tile_px == 32) return launch_lean_k<32>(ctx, P, d_counter, t, s);
+    return launch_lean_k<16>(ctx, P, d_counter, t, s);
+}
+
+}  // namespace vxl

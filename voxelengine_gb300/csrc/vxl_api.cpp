@@ -338,15 +338,30 @@ vxl_status vxl_grid_create(vxl_ctx* ctx, int nx, int ny, int nz, vxl_grid** out)
     g->tz = tz;
     g->nwords = (size_t)nbricks;
     g->nmask = (size_t)((ntiles + 31) / 32);
+    trace_layout_dims(g);
     cudaError_t e = cudaMalloc(&g->words, g->nwords * sizeof(uint64_t));
     if (e == cudaSuccess) e = cudaMalloc(&g->tmask, g->nmask * sizeof(uint32_t));
+    if (e == cudaSuccess && g->tl_nwords) e = cudaMalloc(&g->tl_words, g->tl_nwords * sizeof(uint64_t));
     if (e == cudaSuccess) e = cudaMemset(g->words, 0, g->nwords * sizeof(uint64_t));
-    if (e == cudaSuccess) e = cudaMemset(g->tmask, 0, g->nmask * sizeof(uint32_t));
+    if (e == cudaSuccess && g->tl_nwords) e = cudaMemset(g->tl_words, 0, g->tl_nwords * sizeof(uint64_t));
     if (e != cudaSuccess) {
         if (g->words) cudaFree(g->words);
         if (g->tmask) cudaFree(g->tmask);
+        if (g->tl_words) cudaFree(g->tl_words);
         delete g;
         return cuda_fail(e, "grid_create: device allocation");
+    }
+    vxl_status st = launch_build_tile_mask(g, 0);
+    if (st == VXL_OK) {
+        e = cudaStreamSynchronize(0);
+        if (e != cudaSuccess) st = cuda_fail(e, "grid_create: build");
+    }
+    if (st != VXL_OK) {
+        cudaFree(g->words);
+        cudaFree(g->tmask);
+        if (g->tl_words) cudaFree(g->tl_words);
+        delete g;
+        return st;
     }
     *out = g;
     return VXL_OK;
@@ -357,6 +372,7 @@ vxl_status vxl_grid_destroy(vxl_grid* g) {
     cudaSetDevice(g->device);  // the context may already be gone
     cudaFree(g->words);
     cudaFree(g->tmask);
+    if (g->tl_words) cudaFree(g->tl_words);
     delete g;
     return VXL_OK;
 }
@@ -376,6 +392,12 @@ vxl_status vxl_grid_describe(const vxl_grid* g, vxl_grid_desc* out) {
     out->words_bytes = g->nwords * sizeof(uint64_t);
     out->tile_mask = g->tmask;
     out->tile_mask_bytes = g->nmask * sizeof(uint32_t);
+    out->trace_words = g->tl_words;
+    out->trace_words_bytes = g->tl_nwords * sizeof(uint64_t);
+    out->trace_lbx = g->tl_lbx;
+    out->trace_lby = g->tl_lby;
+    out->trace_bz = g->tl_bz;
+    out->pad = 0;
     return VXL_OK;
 }
 
@@ -383,8 +405,7 @@ vxl_status vxl_grid_clear(vxl_grid* g, void* stream) {
     if (!grid_ok(g)) return fail(VXL_ERR_INVALID_ARG, "grid_clear: bad grid");
     VXL_TRY(set_device(g->ctx));
     VXL_TRY_CUDA(cudaMemsetAsync(g->words, 0, g->nwords * sizeof(uint64_t), (cudaStream_t)stream));
-    VXL_TRY_CUDA(cudaMemsetAsync(g->tmask, 0, g->nmask * sizeof(uint32_t), (cudaStream_t)stream));
-    return VXL_OK;
+    return launch_build_tile_mask(g, (cudaStream_t)stream);
 }
 
 vxl_status vxl_grid_build_bricks(vxl_grid* g, void* stream) {

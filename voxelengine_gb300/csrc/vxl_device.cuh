@@ -70,6 +70,53 @@ __device__ __forceinline__ bool block2_any(const GridView& g, int bx, int by, in
     return ((w >> sh) & 0x0000000000330033ull) != 0ull;
 }
 
+// ---------------------------------------------------------- trace layout
+// The grid as the occlusion traversal reads it (see vxl_grid_desc): cell x at
+// x' = x + 4, brick (x'>>2, y'>>2, z'>>2) at word (x'>>2) + ((y'>>2) << lbx) +
+// ((z'>>2) << (lbx + lby)), bit (x'&3) + 4(y'&3) + 16(z'&3); the cells with a
+// coordinate equal to -1 or n+2 (and all three in [-1, n+2]) are set.
+struct TraceLayout {
+    uint64_t* words;
+    int lbx, lby, bz;
+    int nx, ny, nz;
+};
+
+// The bit address of a cell splits into one term per axis,
+//   A = ax(x') + ay(y') + az(z'),
+//   ax = (x'&3)      | (x'>>2) << 6
+//   ay = (y'&3) << 2 | (y'>>2) << (6 + lbx)
+//   az = (z'&3) << 4 | (z'>>2) << (6 + lbx + lby),
+// whose bit fields do not overlap. A step of one cell along an axis is an add
+// and a mask on that axis's term: the add carries across the bits the other
+// axes use (the gap), the mask clears them again. Masks and increments per
+// axis (index 0 = x, 1 = y, 2 = z):
+struct AxisCode {
+    uint32_t field;  // the bits of A this axis owns
+    uint32_t keep;   // ~gap: the mask applied after each step
+    uint32_t inc;    // increment of a +1 step (gap + unit); a -1 step adds -unit
+    uint32_t unit;
+    int lo_shift;    // position of the axis's two low bits
+    int hi_shift;    // position of its brick index
+};
+__host__ __device__ inline AxisCode axis_code(int axis, int lbx, int lby) {
+    AxisCode c;
+    c.lo_shift = 2 * axis;
+    c.hi_shift = axis == 0 ? 6 : (axis == 1 ? 6 + lbx : 6 + lbx + lby);
+    const uint32_t lo_bits = 3u << c.lo_shift;
+    const uint32_t hi_bits = axis == 2 ? ~((1u << c.hi_shift) - 1u)
+                                       : (((1u << (axis == 0 ? lbx : lby)) - 1u) << c.hi_shift);
+    c.field = lo_bits | hi_bits;
+    const uint32_t gap = ((1u << c.hi_shift) - 1u) & ~((4u << c.lo_shift) - 1u);
+    c.keep = ~gap;
+    c.unit = 1u << c.lo_shift;
+    c.inc = gap + c.unit;
+    return c;
+}
+// the axis term of shifted coordinate v (v >= 0)
+__host__ __device__ inline uint32_t axis_term(const AxisCode& c, int v) {
+    return ((uint32_t)(v & 3) << c.lo_shift) | ((uint32_t)(v >> 2) << c.hi_shift);
+}
+
 // ------------------------------------------------------------------ math
 struct f3 {
     float x, y, z;

@@ -63,6 +63,14 @@ struct vxl_grid {
     size_t nwords;
     uint32_t* tmask;
     size_t nmask;  // uint32 words of the tile map
+    // Trace layout: the same 4^3 bricks with cells shifted by +4 on every
+    // axis, bricks per x row and per y column padded to powers of two
+    // (2^tl_lbx, 2^tl_lby, tl_bz z slabs), and a solid border one cell outside
+    // the DDA's inclusive bounds (cells -1 and n+2). Rebuilt from `words` with
+    // the tile map; NULL when the bit addresses would not fit in 32 bits.
+    uint64_t* tl_words;
+    size_t tl_nwords;
+    int tl_lbx, tl_lby, tl_bz;
 };
 
 namespace vxl {
@@ -103,7 +111,10 @@ struct DevModel {
 vxl_status launch_grid_import_r8(vxl_grid* g, const uint8_t* bytes, cudaStream_t s);
 vxl_status launch_grid_export_r8(const vxl_grid* g, uint8_t* bytes, cudaStream_t s);
 vxl_status launch_grid_import_palette(vxl_grid* g, const uint8_t* pal, int opaque_min, cudaStream_t s);
+// the tile map and the trace layout, from the words
 vxl_status launch_build_tile_mask(vxl_grid* g, cudaStream_t s);
+// sets tl_lbx, tl_lby, tl_bz and tl_nwords (0: no trace layout) from the dims
+void trace_layout_dims(vxl_grid* g);
 vxl_status launch_grid_count(const vxl_grid* g, unsigned long long* d_out, cudaStream_t s);
 vxl_status launch_scene_noise(vxl_grid* g, uint32_t seed, float thresh, float freq, int ground_y, cudaStream_t s);
 vxl_status launch_scene_boxes(vxl_grid* g, uint32_t seed, int nboxes, int smin, int smax, cudaStream_t s);
@@ -138,6 +149,13 @@ vxl_status launch_trace_occlusion_pool(vxl_ctx* ctx, const vxl_grid* g, const vx
                                        const vxl_trace_params* p, const vxl_outputs* out,
                                        unsigned long long* d_counter, const vxl_tuning& tune, cudaStream_t s,
                                        uint32_t pix_base = 0);
+// the same pass on the grid's trace layout (occl_lean.cu): used when the grid has
+// one, no per-ray records are asked for and the exact-leap tuning is off
+bool occl_lean_supported(const vxl_grid* g, const vxl_outputs* out, const vxl_tuning& tune);
+vxl_status launch_trace_occlusion_lean(vxl_ctx* ctx, const vxl_grid* g, const vxl_gbuffer* gb,
+                                       const vxl_trace_params* p, const vxl_outputs* out,
+                                       unsigned long long* d_counter, const vxl_tuning& tune, cudaStream_t s,
+                                       uint32_t pix_base);
 // the work-queue counter for one persistent launch on stream s (see d_counters)
 vxl_status ctx_take_counter(vxl_ctx* ctx, cudaStream_t s, unsigned long long** out);
 // batched occlusion: scene table built on the host, uploaded once, one launch
