@@ -33,6 +33,7 @@ struct LeanGrid {
     uint32_t inc[3];                  // +1 step increment; a -1 step adds -unit
     uint32_t unit[3];
     uint32_t lo[3], span[3];          // axis term of shifted coordinate 4 and the span up to n+5
+    uint32_t one, two27;              // 1 and 2^27 as data: multiply-adds by them stay multiply-adds
     int hs[3];                        // shift of each axis's brick index
 };
 
@@ -56,6 +57,8 @@ LeanGrid lean_grid_of(const vxl_grid* g) {
         L.lo[a] = axis_term(c, 4);
         L.span[a] = axis_term(c, n[a] + 5) - L.lo[a];
     }
+    L.one = 1u;
+    L.two27 = 1u << 27;
     return L;
 }
 
@@ -106,6 +109,116 @@ __device__ __forceinline__ int lean_step(const LeanGrid& L, uint32_t& ax, uint32
     return 0;
 }
 
+// A set cell met by the hot form (lean_batch), with the state of its
+// iteration: a hit (returns true, t in *t) unless the loop had already ended
+// at the previous iteration (totalt >= maxt) or the cell lies on the border,
+// i.e. the bounds test of this iteration fails (Light.frag:53).
+__device__ __forceinline__ bool lean_set_cell(const LeanGrid& L, uint32_t ax, uint32_t ay, uint32_t az, float tx,
+                                              float ty, float tz, float tot, float maxt, float* t) {
+    if (!(tot < maxt)) return false;
+    if (ax - L.lo[0] > L.span[0] || ay - L.lo[1] > L.span[1] || az - L.lo[2] > L.span[2]) return false;
+    const float m = fminf(fminf(tx, ty), tz);
+    const bool bx = tx == m, by = ty == m, bz = tz == m;
+    // dot(t_max, select); +0.0f turns a -0 minimum into the +0 the dot product gives
+    float best = m + 0.0f;
+    if ((bx && (by || bz)) || (by && bz)) {
+        best = (bx ? tx : 0.0f) + (by ? ty : 0.0f);
+        best = best + (bz ? tz : 0.0f);
+    }
+    *t = best;
+    return true;
+}
+
+// The hot form: KSTEP iterations of Light.frag:50-75 as one block of
+// hand-written PTX, for batches that cannot reach the 256-iteration cap.
+// The traversal is bound by the SM's ALU pipe (compares, min/max, logic,
+// shifts, predicate and move operations issue there at half the FMA pipe's
+// rate), so the integer adds and the address shift are multiply-adds by a
+// register holding 1 and a high multiply by 2^27, which run on the FMA pipe,
+// and the per-axis updates run under predicates. Each iteration:
+//   a = ax + ay + az; the cell's bit set -> leave with stop = 1, the state of
+//   this iteration kept (lean_set_cell classifies it);
+//   m = min(t); select = "t_i == m" (step(t.xyz, t.zxy) * step(t.xyz, t.yzx));
+//   the selected axes advance; totalt = m, or on an exact tie (two or more
+//   selected) the sum of the tied components, all equal to m, which is
+//   tested against maxt at once in an out-of-line block (stop = 2 when
+//   reached). After the last iteration stop = 0.
+#define VXL_LEAN_IT(i)                     \
+    "mad.lo.u32 a, %0, %16, %1;\n\t"       \
+    "mad.lo.u32 a, %2, %16, a;\n\t"        \
+    "mul.hi.u32 s, a, %17;\n\t"            \
+    "mad.wide.u32 ad, s, 4, %18;\n\t"      \
+    "ld.global.nc.u32 w, [ad];\n\t"        \
+    "min.f32 m, %3, %4;\n\t"               \
+    "min.f32 m, m, %5;\n\t"                \
+    "setp.eq.f32 px, %3, m;\n\t"           \
+    "setp.eq.f32 py, %4, m;\n\t"           \
+    "setp.eq.f32 pz, %5, m;\n\t"           \
+    "shf.r.wrap.b32 s, w, w, a;\n\t"       \
+    "and.b32 s, s, 1;\n\t"                 \
+    "setp.ne.u32 pb, s, 0;\n\t"            \
+    "@pb bra VXL_SET;\n\t"                 \
+    "@px mad.lo.u32 %0, %11, %16, %0;\n\t" \
+    "@py mad.lo.u32 %1, %12, %16, %1;\n\t" \
+    "@pz mad.lo.u32 %2, %13, %16, %2;\n\t" \
+    "@px and.b32 %0, %0, 0xFFFFFFC3;\n\t"  \
+    "@py and.b32 %1, %1, %14;\n\t"         \
+    "@pz and.b32 %2, %2, %15;\n\t"         \
+    "@px add.rn.f32 %3, %3, %8;\n\t"       \
+    "@py add.rn.f32 %4, %4, %9;\n\t"       \
+    "@pz add.rn.f32 %5, %5, %10;\n\t"      \
+    "and.pred q, px, py;\n\t"              \
+    "and.pred r, px, pz;\n\t"              \
+    "or.pred q, q, r;\n\t"                 \
+    "and.pred r, py, pz;\n\t"              \
+    "or.pred q, q, r;\n\t"                 \
+    "mov.f32 %6, m;\n\t"                   \
+    "@q bra VXL_TIE" #i ";\n"              \
+    "VXL_BACK" #i ":\n\t"
+#define VXL_LEAN_TIE(i)                    \
+    "VXL_TIE" #i ":\n\t"                   \
+    "and.pred r, px, py;\n\t"              \
+    "and.pred r, r, pz;\n\t"               \
+    "add.rn.f32 b, m, m;\n\t"              \
+    "@r add.rn.f32 b, b, m;\n\t"           \
+    "@!r add.rn.f32 b, b, 0f00000000;\n\t" \
+    "setp.lt.f32 pn, b, %19;\n\t"          \
+    "@!pn bra VXL_END;\n\t"                \
+    "mov.f32 %6, b;\n\t"                   \
+    "bra VXL_BACK" #i ";\n"
+#define VXL_LEAN_BLOCK(ITERS, TIES)                                                                      \
+    asm volatile("{\n\t"                                                                                 \
+                 ".reg .pred px, py, pz, pb, q, r, pn;\n\t"                                              \
+                 ".reg .b32 a, s, w;\n\t"                                                                \
+                 ".reg .b64 ad;\n\t"                                                                     \
+                 ".reg .f32 m, b;\n\t" ITERS                                                             \
+                 "mov.u32 %7, 0;\n\t"                                                                    \
+                 "bra VXL_DONE;\n"                                                                       \
+                 "VXL_SET:\n\t"                                                                          \
+                 "mov.u32 %7, 1;\n\t"                                                                    \
+                 "bra VXL_DONE;\n"                                                                       \
+                 "VXL_END:\n\t"                                                                          \
+                 "mov.u32 %7, 2;\n\t"                                                                    \
+                 "bra VXL_DONE;\n" TIES "VXL_DONE:\n\t"                                                  \
+                 "}"                                                                                     \
+                 : "+r"(ax), "+r"(ay), "+r"(az), "+f"(tx), "+f"(ty), "+f"(tz), "+f"(tot), "=r"(stop)     \
+                 : "f"(tdx), "f"(tdy), "f"(tdz), "r"(kx), "r"(ky), "r"(kz), "r"(keep_y), "r"(keep_z),      \
+                   "r"(one), "r"(two27), "l"(w), "f"(maxt))
+#define VXL_LEAN_IT4(o) VXL_LEAN_IT(o##0) VXL_LEAN_IT(o##1) VXL_LEAN_IT(o##2) VXL_LEAN_IT(o##3)
+#define VXL_LEAN_TIE4(o) VXL_LEAN_TIE(o##0) VXL_LEAN_TIE(o##1) VXL_LEAN_TIE(o##2) VXL_LEAN_TIE(o##3)
+
+template <int KSTEP>
+__device__ __forceinline__ int lean_batch(const uint32_t* __restrict__ w, uint32_t& ax, uint32_t& ay, uint32_t& az,
+                                          float& tx, float& ty, float& tz, float tdx, float tdy, float tdz,
+                                          uint32_t kx, uint32_t ky, uint32_t kz, uint32_t keep_y, uint32_t keep_z,
+                                          uint32_t one, uint32_t two27, float maxt, float& tot) {
+    static_assert(KSTEP == 4 || KSTEP == 8, "batch of 4 or 8 iterations");
+    int stop;
+    if (KSTEP == 4) VXL_LEAN_BLOCK(VXL_LEAN_IT4(1), VXL_LEAN_TIE4(1));
+    if (KSTEP == 8) VXL_LEAN_BLOCK(VXL_LEAN_IT4(1) VXL_LEAN_IT4(2), VXL_LEAN_TIE4(1) VXL_LEAN_TIE4(2));
+    return stop;
+}
+
 #ifndef VXL_LEAN_MIN_BLOCKS
 #define VXL_LEAN_MIN_BLOCKS 8
 #endif
@@ -125,6 +238,7 @@ __global__ void __launch_bounds__(128, VXL_LEAN_MIN_BLOCKS) k_occl_lean(const Le
     float* res_t = reinterpret_cast<float*>(wbase + (size_t)TP * R * sizeof(PSlot));
     uint32_t* res_hit = reinterpret_cast<uint32_t*>(wbase + (size_t)TP * R * (sizeof(PSlot) + sizeof(float)));
     const unsigned ux = S.g.ux, uy = S.g.uy, uz = S.g.uz;
+    const uint32_t keep_y = L.keep[1], keep_z = L.keep[2], one = L.one, two27 = L.two27;
     constexpr int LPP = 32 / TP;  // lanes per pixel during generation
 
     for (;;) {
@@ -240,12 +354,13 @@ __global__ void __launch_bounds__(128, VXL_LEAN_MIN_BLOCKS) k_occl_lean(const Le
                     int res = 0;
                     float ht = 0.0f;
                     if (__all_sync(__activemask(), n + KSTEP <= 256)) {
-#pragma unroll
-                        for (int it = 0; it < KSTEP; it++) {
-                            res = lean_step(L, ax, ay, az, tx, ty, tz, tdx, tdy, tdz, kx, ky, kz, maxt, tot, &ht);
-                            if (res) break;
-                        }
-                        if (!res) {
+                        const int st = lean_batch<KSTEP>(L.w, ax, ay, az, tx, ty, tz, tdx, tdy, tdz, kx, ky, kz,
+                                                         keep_y, keep_z, one, two27, maxt, tot);
+                        if (st == 1)
+                            res = lean_set_cell(L, ax, ay, az, tx, ty, tz, tot, maxt, &ht) ? 1 : 2;
+                        else if (st == 2)
+                            res = 2;
+                        else {
                             n += KSTEP;
                             if (!(tot < maxt)) res = 2;
                         }
@@ -343,8 +458,9 @@ template <int TP>
 static vxl_status launch_lean_k(vxl_ctx* ctx, const LeanScene& P, unsigned long long* counter, const vxl_tuning& t,
                                 cudaStream_t s) {
     switch (t.kstep) {
+        case 1:
+        case 2:
         case 4: return launch_lean_t<TP, 4>(ctx, P, counter, t.grab, s);
-        case 16: return launch_lean_t<TP, 16>(ctx, P, counter, t.grab, s);
         default: return launch_lean_t<TP, 8>(ctx, P, counter, t.grab, s);
     }
 }
