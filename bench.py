@@ -56,32 +56,28 @@ def light_dir(seed):
     return (v / np.linalg.norm(v)).astype(np.float32)
 
 
-def profiled_traffic(workload):
-    """DRAM bytes per launch of the occlusion kernel from the committed ncu
-    summary of this workload (profiles/k_occl_pool_<workload>.md), or None."""
-    p = os.path.join(ROOT, "profiles", "k_occl_pool_%s.md" % workload)
+def kernel_profile(workload):
+    """Figures of the occlusion kernel from the committed ncu summary of this
+    workload (profiles/k_occl_lean_<workload>.md): the kernel it covers, DRAM
+    and L2 bytes per launch and pipe utilisation, or None where absent."""
+    p = os.path.join(ROOT, "profiles", "k_occl_lean_%s.md" % workload)
     if not os.path.exists(p):
         return None
+    out = {"file": os.path.relpath(p, ROOT)}
     for line in open(p):
-        if line.startswith("traffic_bytes_per_launch:"):
-            return int(line.split(":")[1])
-    return None
-
-
-def profiled_pipes(workload):
-    """ALU-pipe and issue-slot utilisation (fractions) of the occlusion kernel
-    from the committed full ncu capture of this workload, or None: the kernel
-    is issue/ALU-bound, which the HBM fraction alone does not show."""
-    p = os.path.join(ROOT, "profiles", "k_occl_pool_%s.md" % workload)
-    if not os.path.exists(p):
-        return None
-    out = {}
-    for line in open(p):
+        for key in ("kernel", "traffic_bytes_per_launch", "l2_bytes_per_launch"):
+            if line.startswith(key + ":"):
+                v = line.split(":", 1)[1].strip()
+                out[key] = int(v) if key != "kernel" else v
         for key, name in (("sm__pipe_alu_cycles_active.avg.pct_of_peak_sustained_active", "alu_pipe"),
-                          ("smsp__issue_active.avg.pct_of_peak_sustained_active", "issue_active")):
+                          ("smsp__issue_active.avg.pct_of_peak_sustained_active", "issue_active"),
+                          ("smsp__sass_branch_targets_threads_divergent.sum", "divergent_branch_targets"),
+                          ("smsp__thread_inst_executed_per_inst_executed.ratio", "threads_per_instruction"),
+                          ("sm__warps_active.avg.pct_of_peak_sustained_active", "warps_active")):
             if line.startswith("| `%s` |" % key):
-                out[name] = float(line.split("|")[2].split()[0]) / 100.0
-    return out or None
+                v = float(line.split("|")[2].split()[0])
+                out[name] = v / 100.0 if "pct" in key else v
+    return out
 
 
 def measured_peaks():
@@ -419,11 +415,14 @@ def run_gpu(args, wl):
     if rank != 0:
         return
     hbm, peak_kind = measured_peaks()
+    # the L2 side: this GPU's L2 read bandwidth, measured here by a streaming kernel
+    l2_gbs, l2_ms = V.l2_read_gbs(ctx, 64 << 20, 50)
     b_pix_in = 24 + (4 if wl["n_spec"] else 0)
     b_pix_out = 4 * 5
     b_ray = (b_pix_in + b_pix_out) / R + 4.0 * s_ref
     ms = statistics.mean(times)
     achieved = b_ray * rays_per_step / (ms / 1e3) / 1e9
+    prof = kernel_profile(args.workload)
     line = {
         "metric": "Grays/s shadow+AO+spec occlusion (exact voxel DDA)", "value": value, "unit": "Grays/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -433,13 +432,16 @@ def run_gpu(args, wl):
         "rays_per_step": rays_per_step, "valid_pixels": valid, "s_ref_mean_fetches_per_ray": s_ref,
         "hit_fraction": hits,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": profiled_traffic(args.workload), "peak_kind": peak_kind,
-                     "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one launch, "
-                                       "profiles/k_occl_pool_%s.md" % args.workload,
+                     "frac_hbm": achieved / hbm, "l2_peak": l2_gbs, "frac_l2": achieved / l2_gbs,
+                     "l2_peak_how": "best of 50 timed reads of a 64 MiB L2-resident buffer (vxl_diag_l2_read_gbs), "
+                                    "this run",
+                     "traffic": prof.get("traffic_bytes_per_launch") if prof else None,
+                     "l2_traffic": prof.get("l2_bytes_per_launch") if prof else None,
+                     "peak_kind": peak_kind, "profile": prof,
                      "bytes_per_ray": b_ray,
-                     "ncu_pipes": profiled_pipes(args.workload),
                      "note": "algorithmic bytes = ((28 B in + 20 B out) per pixel)/R + 4 B x S_ref per ray; "
-                             "per-launch time from CUDA events on the launch stream"},
+                             "per-launch time from CUDA events on the launch stream; traffic from the ncu "
+                             "summary named in profile"},
         "e2e": {"value": e2e, "unit": "Grays/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "vxl_trace_occlusion_host, pinned host G-buffer and outputs"},
         "gpu_launches": int(launches),
@@ -471,16 +473,32 @@ def run_gpu(args, wl):
                                                   budget_s=min(4.0, args.cpu_seconds), threads=1)
         line["cpu_baseline"]["one_core"] = {"value": v1 / 1e9, "unit": "Grays/s", "cores": 1,
                                             "sample": "%d whole image rows (%.1f s)" % (rows1, dt1)}
+    if not args.no_extras and args.workload == "c2":
+        # the batched and differentiable forms, compact, on the same GPU
+        n_ex = max(3, min(args.steps, 10))
+        c3 = c3_result(args, n_ex, 3, check=not args.no_cpu_baseline)
+        line["c3_batched"] = {k: c3[k] for k in ("value", "unit", "ms_per_step", "plain_value", "plain_ms_per_step",
+                                                 "batched_over_plain", "rays_per_step", "clocks")}
+        line["c3_batched"]["voxelize_gvoxels_per_s"] = c3["voxelize"]["gvoxels_per_s"]
+        if "oracle_check" in c3:
+            line["c3_batched"]["oracle_check"] = c3["oracle_check"]
+        c4 = c4_result(args, n_ex, 3, fd_check=not args.no_cpu_baseline, cpu_baseline=False)
+        line["c4_adjoint"] = {k: c4[k] for k in ("value", "unit", "forward_ms", "adjoint_ms", "adjoint_over_forward",
+                                                 "clocks")}
+        if "fd_check" in c4:
+            line["c4_adjoint"]["fd_check"] = c4["fd_check"]
     print(json.dumps(line))
 
 
-def run_gpu_c3(args):
+def c3_result(args, steps, warmup, check=True):
     """C3: 64 scenes (edges log-uniform 64-512, noise threshold U[0.45,0.65],
     rays per scene log-uniform 64K-2M at 1 shadow + 8 AO + 1 spec per pixel),
     10,000 Vox instances (edge 8-64, ~40% fill, uniform rotations) voxelized
     into the scene grids first (timed on its own). One step = all 64 scenes:
     the batched form (one persistent launch, CUDA-graph replay) against the
-    plain form (one vxl_trace_occlusion per scene)."""
+    plain form (one vxl_trace_occlusion per scene). With `check`, the batch's
+    output buffers of 8 of the scenes are compared with the oracle on bands
+    of their image rows."""
     import torch
 
     import voxelengine_gb300 as V
@@ -522,7 +540,7 @@ def run_gpu_c3(args):
                               shadow=sc["shadow"], ao=sc["ao"], ao_vis=sc["ao_vis"], spec=sc["spec"],
                               spec_t=sc["spec_t"])
 
-    if args.autotune:
+    if getattr(args, "autotune", False):
         def make_step():
             b = V.Batch(ctx, scenes, use_graph=True)
             return b.run
@@ -532,11 +550,11 @@ def run_gpu_c3(args):
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
 
     def timed(fn):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             fn()
         torch.cuda.synchronize()
         ts = []
-        for s in range(args.steps):
+        for s in range(steps):
             flush.fill_(float(s))
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record()
@@ -544,36 +562,78 @@ def run_gpu_c3(args):
             b.record()
             ts.append((a, b))
         torch.cuda.synchronize()
-        return sum(a.elapsed_time(b) for a, b in ts) / 1e3 / args.steps
+        return sum(a.elapsed_time(b) for a, b in ts) / 1e3 / steps
 
     with ClockSampler(0) as clk:
         t_plain = timed(plain)
         t_batch = timed(batch.run)
-    line = {
-        "metric": "Grays/s shadow+AO+spec occlusion, 64-scene batch (exact voxel DDA)",
-        "value": traced / t_batch / 1e9, "unit": "Grays/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": t_batch * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic (seeded scenes, G-buffers and Vox instances)",
-        "config": {"workload": "batch-64-scenes", "edges": [int(sc["n"]) for sc in scenes],
-                   "pixels": [int(sc["npix"]) for sc in scenes], "rays_per_pixel": 10, "instances": 10000,
-                   "l2": "flushed between timed steps"},
+    out = {
+        "value": traced / t_batch / 1e9, "unit": "Grays/s", "ms_per_step": t_batch * 1e3,
         "plain_value": traced / t_plain / 1e9, "plain_ms_per_step": t_plain * 1e3,
         "batched_over_plain": t_plain / t_batch, "rays_per_step": traced, "rays_nominal": rays,
+        "edges": [int(sc["n"]) for sc in scenes], "pixels": [int(sc["npix"]) for sc in scenes],
         "voxelize": {"seconds": t_vox, "instances": 10000, "source_voxels": src_voxels,
                      "gvoxels_per_s": src_voxels / t_vox / 1e9},
         "tuning": ctx.get_tuning(), "clocks": clk.summary(),
     }
+    if check:
+        # the last batch run's buffers against the oracle, on bands of rows of every 8th scene
+        batch.run()
+        torch.cuda.synchronize()
+        import ctypes
+
+        import oracle
+
+        chk = {"scenes": [], "values": 0, "bit_mismatches": 0}
+        for i in range(0, len(scenes), 8):
+            sc = scenes[i]
+            n, W, H = sc["n"], sc["W"], sc["H"]
+            g8 = torch.zeros((n // 2) ** 3, dtype=torch.uint8, device="cuda")
+            sc["grid"].export_r8(g8)
+            torch.cuda.synchronize()
+            g_np = g8.cpu().numpy().reshape(n // 2, n // 2, n // 2)
+            op = oracle.Params()
+            ctypes.memmove(ctypes.byref(op), ctypes.byref(sc["params"]), ctypes.sizeof(op))
+            pos, nrm, rough = sc["pos"].cpu().numpy(), sc["nrm"].cpu().numpy(), sc["rough"].cpu().numpy()
+            bands = [(int(y), int(min(H, y + 16))) for y in np.linspace(0, max(0, H - 16), 4).astype(int)]
+            for y0, y1 in sorted(set(bands)):
+                o = oracle.occlusion_range(g_np, pos, nrm, rough, op, y0 * W, y1 * W)
+                for k in ("shadow", "ao", "ao_vis", "spec", "spec_t"):
+                    a = sc[k][y0 * W:y1 * W].cpu().numpy()
+                    w = o[k]
+                    same = (a.view(np.int32) == w.view(np.int32)) | (np.isnan(a) & np.isnan(w))
+                    chk["values"] += a.size
+                    chk["bit_mismatches"] += int((~same).sum())
+            chk["scenes"].append(i)
+        chk["sample"] = "4 bands of 16 image rows of every 8th scene, all five buffers of the batched run"
+        out["oracle_check"] = chk
+    batch.close()
+    return out
+
+
+def run_gpu_c3(args):
+    r = c3_result(args, args.steps, args.warmup, check=not args.no_cpu_baseline)
+    line = {
+        "metric": "Grays/s shadow+AO+spec occlusion, 64-scene batch (exact voxel DDA)",
+        "value": r["value"], "unit": "Grays/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded scenes, G-buffers and Vox instances)",
+        "config": {"workload": "batch-64-scenes", "edges": r.pop("edges"), "pixels": r.pop("pixels"),
+                   "rays_per_pixel": 10, "instances": 10000, "l2": "flushed between timed steps"},
+    }
+    line.update({k: v for k, v in r.items() if k not in ("value", "unit", "ms_per_step")})
     print(json.dumps(line))
 
 
-def run_gpu_c4(args):
+def c4_result(args, steps, warmup, fd_check=True, cpu_baseline=True):
     """C4, the differentiable variant: 128^3 soft grid (opacity
     sigmoid(8 (noise - 0.55)), albedo U[0,1)), 512x512 G-buffer of the matching
     binary scene, 1 shadow + 16 AO rays per pixel of length 24; loss = MSE
     against a target rendered with a second albedo seed. One step = forward,
     dL/dimage, zeroing the gradient and the adjoint. Reports the forward and
-    adjoint times and their ratio; the CPU baseline is the FP64 oracle
-    (forward + adjoint) on a pixel sample."""
+    adjoint times and their ratio. With `fd_check`, the adjoint of a loss on
+    every 64th pixel is compared with FP64 central finite differences
+    (h = 1e-4, the oracle) at the 64 voxels of largest gradient."""
     import torch
 
     import voxelengine_gb300 as V
@@ -611,11 +671,11 @@ def run_gpu_c4(args):
         bwd()
 
     def timed(fn):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             fn()
         torch.cuda.synchronize()
         ts = []
-        for k in range(args.steps):
+        for k in range(steps):
             flush.fill_(float(k))
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record()
@@ -623,7 +683,7 @@ def run_gpu_c4(args):
             b.record()
             ts.append((a, b))
         torch.cuda.synchronize()
-        return sum(a.elapsed_time(b) for a, b in ts) / 1e3 / args.steps
+        return sum(a.elapsed_time(b) for a, b in ts) / 1e3 / steps
 
     step()
     with ClockSampler(0) as clk:
@@ -631,31 +691,69 @@ def run_gpu_c4(args):
         t_bwd = timed(bwd)
         t_step = timed(step)
     loss = float(((img - target) ** 2).mean())
-    line = {
-        "metric": "Grays/s soft-opacity forward + adjoint (exact voxel DDA cells)",
-        "value": rays / t_step / 1e9, "unit": "Grays/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic (seeded soft grid and G-buffer)",
-        "config": {"workload": "soft-128^3-512x512-1shadow+16ao(L24)-mse", "l2": "flushed between timed steps"},
-        "forward_ms": t_fwd * 1e3, "adjoint_ms": t_bwd * 1e3, "adjoint_over_forward": t_bwd / t_fwd,
-        "rays_per_step": rays, "loss": loss, "gpu_launches": 2, "clocks": clk.summary(),
-    }
-    if not args.no_cpu_baseline:
+    out = {"value": rays / t_step / 1e9, "unit": "Grays/s", "ms_per_step": t_step * 1e3,
+           "forward_ms": t_fwd * 1e3, "adjoint_ms": t_bwd * 1e3, "adjoint_over_forward": t_bwd / t_fwd,
+           "rays_per_step": rays, "loss": loss, "clocks": clk.summary()}
+    if fd_check or cpu_baseline:
         import oracle
 
         vox = sc["soft"].cpu().numpy()
         pos, nrm = sc["pos3"].cpu().numpy(), sc["nrm3"].cpu().numpy()
-        gih = gi.cpu().numpy()
         op = oracle.make_soft_params(light_dir=list(P.light_dir), bias=P.bias, length=P.len, k_sun=P.k_sun,
                                      k_amb=P.k_amb, n_shadow=P.n_shadow, n_ao=P.n_ao, seed=P.seed)
         sel = np.arange(0, npix, 64)
+    if fd_check:
+        # the adjoint of L = sum(image[sel] * g) for a seeded g on every 64th pixel
+        rng = np.random.default_rng(5)
+        g_sel = rng.standard_normal((len(sel), 3)).astype(np.float32)
+        g_full = np.zeros((npix, 3), np.float32)
+        g_full[sel] = g_sel
+        fwd()
+        gi.copy_(torch.from_numpy(g_full))
+        grad.zero_()
+        bwd()
+        torch.cuda.synchronize()
+        got = grad.cpu().numpy()[..., 0].ravel().astype(np.float64)
+        a = vox[..., 0].ravel()
+        amax = 1.0 - 1.0 / 4096.0
+        cand = np.flatnonzero((a > 2e-4) & (a < amax - 2e-4) & (got != 0))
+        pick = cand[np.argsort(-np.abs(got[cand]))[:64]]
+        h = 1e-4
+        threads = os.cpu_count() or 1
+
+        def lossv(v, d):
+            return float((oracle.soft_render(vox, pos[sel], nrm[sel], op, perturb_voxel=v, perturb_delta=d,
+                                             threads=threads) * g_sel).sum())
+
+        fd = np.array([(lossv(v, h) - lossv(v, -h)) / (2 * h) for v in pick])
+        err = np.abs(got[pick] - fd) / np.maximum(np.abs(fd), 1e-3 * np.abs(fd).max())
+        out["fd_check"] = {"voxels": int(len(pick)), "max_rel_err": float(err.max()), "h": h,
+                           "sample": "opacity gradient of a loss on every 64th pixel, 64 voxels of largest "
+                                     "gradient, FP64 central differences by the oracle"}
+    if cpu_baseline:
+        gih = gi.cpu().numpy()
         live = int((np.abs(nrm[sel]).sum(1) > 0).sum())
         threads = min(4, os.cpu_count() or 1)
         t0 = time.perf_counter()
         oracle.soft_render(vox, pos[sel], nrm[sel], op, gih[sel], threads=threads)
         t = time.perf_counter() - t0
-        line["cpu_baseline"] = {"value": live * 17 / t / 1e9, "unit": "Grays/s", "cores": threads, "kind": "port",
-                                "sample": "FP64 oracle forward+adjoint on every 64th pixel (%d rays)" % (live * 17)}
+        out["cpu_baseline"] = {"value": live * 17 / t / 1e9, "unit": "Grays/s", "cores": threads, "kind": "port",
+                               "sample": "FP64 oracle forward+adjoint on every 64th pixel (%d rays)" % (live * 17)}
+    return out
+
+
+def run_gpu_c4(args):
+    r = c4_result(args, args.steps, args.warmup, fd_check=not args.no_cpu_baseline,
+                  cpu_baseline=not args.no_cpu_baseline)
+    line = {
+        "metric": "Grays/s soft-opacity forward + adjoint (exact voxel DDA cells)",
+        "value": r["value"], "unit": "Grays/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded soft grid and G-buffer)",
+        "config": {"workload": "soft-128^3-512x512-1shadow+16ao(L24)-mse", "l2": "flushed between timed steps"},
+        "gpu_launches": 2,
+    }
+    line.update({k: v for k, v in r.items() if k not in ("value", "unit", "ms_per_step")})
     print(json.dumps(line))
 
 
@@ -807,6 +905,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="leave the C3 batched and C4 adjoint figures out of "
+                                                              "the default line")
     ap.add_argument("--tuning", default="", help="tile_px,kstep,leap,order,tile_w,grab for the occlusion kernel")
     ap.add_argument("--autotune", action="store_true", help="search the launch shape first and cache it")
     args = ap.parse_args()

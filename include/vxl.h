@@ -93,7 +93,7 @@ vxl_status vxl_ctx_launch_count(const vxl_ctx* ctx, uint64_t* out);
  * Zero fields keep the current value. Picked per device by the autotuner
  * (voxelengine_gb300/autotune.py). */
 typedef struct vxl_tuning {
-    int32_t tile_px;   /* pixels per warp tile: 16 or 32 */
+    int32_t tile_px;   /* pixels per warp tile: 8, 16 or 32 (the exact-step and batched kernels run 8 as 16) */
     int32_t kstep;     /* DDA iterations between pool refills: 1, 2, 4 or 8 */
     int32_t leap;      /* 1: cross empty bricks in one step where exact; 2: never */
     int32_t order;     /* 1: dispatch spec, shadow, AO; 2: shadow, AO, spec */
@@ -631,6 +631,15 @@ vxl_status vxl_scene_boxes(vxl_ctx* ctx, vxl_grid* grid, uint32_t seed, int nbox
 vxl_status vxl_scene_gbuffer(vxl_ctx* ctx, const vxl_grid* grid, const float cam[3], const float target[3],
                              float tan_half_fov, int W, int H, uint32_t seed, float* d_pos, float* d_nrm,
                              float* d_rough, void* stream);
+
+/* ------------------------------------------------------------ diagnostics
+ * No counterpart in the reference. The L2 read bandwidth of this GPU: a
+ * kernel streams a device buffer of `bytes` (at least 1 MiB, a multiple of
+ * 16; it allocates it and frees it again), small enough to stay in L2,
+ * `reps` timed times after three untimed ones; the best time gives GB/s.
+ * Synchronous. The occlusion benchmark reports its roofline against it for
+ * grids that stay in L2. */
+vxl_status vxl_diag_l2_read_gbs(vxl_ctx* ctx, size_t bytes, int reps, double* best_gbs, double* best_ms);
 
 #ifdef __cplusplus
 }

@@ -46,6 +46,7 @@ EXPORTED = [
     "vxl_prefab_renderer_at", "vxl_prefab_volume_at", "vxl_prefab_palette_at", "vxl_prefab_destroy",
     "vxl_vox_load", "vxl_vox_info", "vxl_vox_model_at", "vxl_vox_palette", "vxl_vox_destroy",
     "vxl_read_v", "vxl_scene_soft", "vxl_scene_terrain", "vxl_scene_noise", "vxl_scene_boxes", "vxl_scene_gbuffer",
+    "vxl_diag_l2_read_gbs",
 ]
 
 
@@ -201,6 +202,7 @@ def lib():
         L.vxl_light_taa.argtypes = [vp, C.POINTER(TaaFrame), vp, vp]
         L.vxl_light_points.argtypes = [vp, vp, vp, vp, vp, i64, C.POINTER(Light), C.c_int, vp, vp, vp]
         L.vxl_voxelize.argtypes = [vp, vp, C.POINTER(Model), C.c_int, C.POINTER(Instance), C.c_int, vp, vp]
+        L.vxl_diag_l2_read_gbs.argtypes = [vp, C.c_size_t, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.vxl_voxelize_noalloc.argtypes = [C.POINTER(GridDesc), C.POINTER(Model), C.c_int, C.POINTER(Instance),
                                            C.c_int, vp, vp]
         L.vxl_shadowvox_update.argtypes = [vp, vp, C.POINTER(Model), C.c_int, C.POINTER(Entity), C.c_int, vp, vp]
@@ -745,3 +747,11 @@ def read_v(path: str) -> np.ndarray:
     out = np.zeros((sz.value, sy.value, sx.value), np.uint8)
     check(lib().vxl_read_v(path.encode(), C.byref(sx), C.byref(sy), C.byref(sz), _ptr(out), out.nbytes))
     return out
+
+
+def l2_read_gbs(ctx: Context, nbytes: int = 64 << 20, reps: int = 50):
+    """Best L2 read bandwidth (GB/s, ms) of a kernel streaming an
+    L2-resident buffer of nbytes (vxl_diag_l2_read_gbs)."""
+    g, ms = C.c_double(), C.c_double()
+    check(lib().vxl_diag_l2_read_gbs(ctx.handle, nbytes, reps, C.byref(g), C.byref(ms)))
+    return g.value, ms.value

@@ -22,6 +22,8 @@
 //    lane takes past its ray's end only touch cells inside the border.
 //  - The 256-iteration cap (Light.frag:75) is tested per batch: a batch that
 //    might reach it runs the iterations with the cap and maxt tests in place.
+#include <algorithm>
+
 #include "occl_common.cuh"
 
 namespace vxl {
@@ -223,215 +225,253 @@ __device__ __forceinline__ int lean_batch(const uint32_t* __restrict__ w, uint32
 #define VXL_LEAN_MIN_BLOCKS 8
 #endif
 
+// One tile of TP pixels of one scene: generation into the warp's pool,
+// traversal, fold (the phases of the pooled kernels in occlusion.cu).
+template <int TP, int KSTEP>
+__device__ __forceinline__ void lean_tile(const SceneDesc& S, const LeanGrid& L, int64_t tile, PSlot* slots,
+                                          float* res_t, uint32_t* res_hit, int lane) {
+    const TraceConstsP& c = S.c;
+    const int R = c.R;
+    const unsigned ux = S.g.ux, uy = S.g.uy, uz = S.g.uz;
+    const uint32_t keep_y = L.keep[1], keep_z = L.keep[2], one = L.one, two27 = L.two27;
+    constexpr int LPP = 32 / TP;  // lanes per pixel during generation
+    // ------------------------------------------------ A: generation
+    const int p = lane % TP;
+    int64_t gpix;
+    const bool inimg = tile_pixel<TP>(S, tile, p, &gpix);
+    f3 Pp = mk(0.0f, 0.0f, 0.0f), N = mk(0.0f, 0.0f, 0.0f);
+    float ro = c.default_rough;
+    if (inimg) {
+        Pp = ld3(S.pos + 3 * gpix);
+        N = ld3(S.nrm + 3 * gpix);
+        if (S.rough) ro = S.rough[gpix];
+    }
+    const bool sky = !inimg || (N.x == 0.0f && N.y == 0.0f && N.z == 0.0f);
+    const f3 O = add(Pp, mul(N, c.bias));
+    f3 T, B;
+    tangent_frame(N, &T, &B);
+    for (int k = lane; k < R; k += 32) res_hit[k] = 0u;
+    int live = 0;
+    const int rounds = (R + LPP - 1) / LPP;
+    for (int j = 0; j < rounds; j++) {
+        const int kk = j * LPP + lane / TP;
+        const int k = !c.spec_first ? kk : (kk < c.n_spec ? c.n_shadow + c.n_ao + kk : kk - c.n_spec);
+        bool is_live = false;
+        PSlot sl;
+        if (kk < R && !sky) {
+            const f3 d = gen_dir(c, k, (uint32_t)gpix + S.pix_base, Pp, N, T, B, ro);
+            const float maxt = kind_maxt(c, k);
+            const int meta = (p << 4) | (k << 9);
+            if (!ray_domain_ok(O, d)) {
+                // no traversal: a miss
+            } else if (!dir_fast_ok(d)) {
+                is_live = true;
+                sl.c01 = 0;
+                sl.c2m = (meta | kMetaLit) << 16;
+                sl.a0 = O.x; sl.a1 = O.y; sl.a2 = O.z;
+                sl.b0 = d.x; sl.b1 = d.y; sl.b2 = d.z;
+            } else {
+                DState s;
+                dda_init(s, O, d, maxt);
+                // an origin cell outside the bounds ends the ray at the first test (Light.frag:53)
+                if ((unsigned)s.cx <= ux && (unsigned)s.cy <= uy && (unsigned)s.cz <= uz) {
+                    is_live = true;
+                    const int sg = (s.sx < 0 ? 1 : 0) | (s.sy < 0 ? 2 : 0) | (s.sz < 0 ? 4 : 0);
+                    const uint32_t xs = (uint32_t)(s.cx + 4), ys = (uint32_t)(s.cy + 4), zs = (uint32_t)(s.cz + 4);
+                    sl.c01 = (int)((xs & 3u) | ((xs >> 2) << L.hs[0]) | ((ys & 3u) << 2) | ((ys >> 2) << L.hs[1]) |
+                                   ((zs & 3u) << 4) | ((zs >> 2) << L.hs[2]));
+                    sl.c2m = (meta | sg) << 16;
+                    sl.a0 = s.tx; sl.a1 = s.ty; sl.a2 = s.tz;
+                    sl.b0 = s.tdx; sl.b1 = s.tdy; sl.b2 = s.tdz;
+                }
+            }
+        }
+        const unsigned lv = __ballot_sync(0xffffffffu, is_live);
+        if (is_live) slots[live + __popc(lv & lanes_below())] = sl;
+        live += __popc(lv);
+    }
+    __syncwarp();
+
+    // ------------------------------------------------- B: traversal
+    int base = 0;
+    bool busy = false, retired = false;
+    uint32_t ax = 0, ay = 0, az = 0, kx = 0, ky = 0, kz = 0;
+    float tx = 0.0f, ty = 0.0f, tz = 0.0f, tdx = 0.0f, tdy = 0.0f, tdz = 0.0f, maxt = 0.0f, tot = 0.0f;
+    int n = 0, meta = 0;
+    for (;;) {
+        const bool need = !busy && !retired;
+        const unsigned nm = __ballot_sync(0xffffffffu, need);
+        if (nm) {
+            if (need) {
+                const int at = base + __popc(nm & lanes_below());
+                if (at < live) {
+                    const PSlot sl = slots[at];
+                    meta = (unsigned)sl.c2m >> 16;
+                    const int k = (meta >> 9) & 31;
+                    maxt = kind_maxt(c, k);
+                    if (meta & kMetaLit) {
+                        const Hit h = dda_literal(S.g, mk(sl.a0, sl.a1, sl.a2), mk(sl.b0, sl.b1, sl.b2), maxt);
+                        if (h.flags & VXL_RF_HIT) {
+                            const int pp = (meta >> 4) & 31;
+                            res_t[k * TP + pp] = h.t;
+                            atomicOr(&res_hit[k], 1u << pp);
+                        }
+                    } else {
+                        busy = true;
+                        const uint32_t A = (uint32_t)sl.c01;
+                        ax = A & L.field[0];
+                        ay = A & L.field[1];
+                        az = A & L.field[2];
+                        kx = (meta & 1) ? 0u - L.unit[0] : L.inc[0];
+                        ky = (meta & 2) ? 0u - L.unit[1] : L.inc[1];
+                        kz = (meta & 4) ? 0u - L.unit[2] : L.inc[2];
+                        tx = sl.a0; ty = sl.a1; tz = sl.a2;
+                        tdx = sl.b0; tdy = sl.b1; tdz = sl.b2;
+                        tot = -INFINITY;
+                        n = 0;
+                    }
+                } else {
+                    retired = true;
+                }
+            }
+            base += __popc(nm);
+        }
+        if (!__any_sync(0xffffffffu, busy) && base >= live) break;
+        if (busy) {
+            int res = 0;
+            float ht = 0.0f;
+            if (__all_sync(__activemask(), n + KSTEP <= 256)) {
+                const int st = lean_batch<KSTEP>(L.w, ax, ay, az, tx, ty, tz, tdx, tdy, tdz, kx, ky, kz,
+                                                 keep_y, keep_z, one, two27, maxt, tot);
+                if (st == 1)
+                    res = lean_set_cell(L, ax, ay, az, tx, ty, tz, tot, maxt, &ht) ? 1 : 2;
+                else if (st == 2)
+                    res = 2;
+                else {
+                    n += KSTEP;
+                    if (!(tot < maxt)) res = 2;
+                }
+            } else {
+                // the batch may reach the 256-iteration cap: test it, and maxt, at every iteration
+                for (int it = 0; it < KSTEP; it++) {
+                    if (n >= 256) {
+                        res = 2;
+                        break;
+                    }
+                    res = lean_step(L, ax, ay, az, tx, ty, tz, tdx, tdy, tdz, kx, ky, kz, maxt, tot, &ht);
+                    if (res) break;
+                    n++;
+                    if (!(tot < maxt) || n >= 256) {
+                        res = 2;
+                        break;
+                    }
+                }
+            }
+            if (res) {
+                if (res == 1) {
+                    const int k = (meta >> 9) & 31, pp = (meta >> 4) & 31;
+                    res_t[k * TP + pp] = ht;
+                    atomicOr(&res_hit[k], 1u << pp);
+                }
+                busy = false;
+            }
+        }
+    }
+    __syncwarp();
+
+    // ------------------------------------------------------ C: fold
+    if (lane < TP && inimg) {
+        float sh = 1.0f, ao = 1.0f, vis = 1.0f, sp = 1.0f, st = c.spec_len;
+        if (!sky) {
+            int k = 0;
+            if (c.n_shadow > 0) {
+                sh = ((res_hit[0] >> p) & 1u) ? 0.0f : 1.0f;
+                k = 1;
+            }
+            float acc = 0.0f, v = 0.0f;
+            for (int j = 0; j < c.n_ao; j++, k++) {
+                const bool hit = (res_hit[k] >> p) & 1u;
+                const float t = res_t[k * TP + p];
+                float tt = hit ? (t < c.ao_len ? t : c.ao_len) : c.ao_len;
+                float q = tt / c.ao_len;
+                acc += q * q;
+                v += hit ? 0.0f : 1.0f;
+            }
+            if (c.n_ao > 0) {
+                ao = acc / (float)c.n_ao;
+                vis = v / (float)c.n_ao;
+            }
+            if (c.n_spec > 0) {
+                float spa = 0.0f, sta = 0.0f;
+                for (int j = 0; j < c.n_spec; j++, k++) {
+                    const bool hit = (res_hit[k] >> p) & 1u;
+                    spa += hit ? 0.0f : 1.0f;
+                    sta += hit ? res_t[k * TP + p] : c.spec_len;
+                }
+                sp = spa / (float)c.n_spec;
+                st = sta / (float)c.n_spec;
+            }
+        }
+        if (S.o_shadow) S.o_shadow[gpix] = sh;
+        if (S.o_ao) S.o_ao[gpix] = ao;
+        if (S.o_vis) S.o_vis[gpix] = vis;
+        if (S.o_spec) S.o_spec[gpix] = sp;
+        if (S.o_spec_t) S.o_spec_t[gpix] = st;
+    }
+    __syncwarp();
+}
+
+// one scene; its descriptor lives in kernel parameter space
 template <int TP, int KSTEP>
 __global__ void __launch_bounds__(128, VXL_LEAN_MIN_BLOCKS) k_occl_lean(const LeanScene P,
                                                                         unsigned long long* __restrict__ counter,
                                                                         int grab) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const SceneDesc& S = P.S;
-    const LeanGrid& L = P.L;
-    const TraceConstsP& c = S.c;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int R = c.R;
+    const int R = P.S.c.R;
     unsigned char* wbase = smem + warp * pool_bytes(TP, R);
     PSlot* slots = reinterpret_cast<PSlot*>(wbase);
     float* res_t = reinterpret_cast<float*>(wbase + (size_t)TP * R * sizeof(PSlot));
     uint32_t* res_hit = reinterpret_cast<uint32_t*>(wbase + (size_t)TP * R * (sizeof(PSlot) + sizeof(float)));
-    const unsigned ux = S.g.ux, uy = S.g.uy, uz = S.g.uz;
-    const uint32_t keep_y = L.keep[1], keep_z = L.keep[2], one = L.one, two27 = L.two27;
-    constexpr int LPP = 32 / TP;  // lanes per pixel during generation
-
     for (;;) {
         int64_t t0 = 0;
         if (lane == 0) t0 = (int64_t)atomicAdd(counter, (unsigned long long)grab);
         t0 = __shfl_sync(0xffffffffu, t0, 0);
-        if (t0 >= S.ntiles) break;
-        for (int gi = 0; gi < grab && t0 + gi < S.ntiles; gi++) {
-            const int64_t tile = t0 + gi;
-            // ------------------------------------------------ A: generation
-            const int p = lane % TP;
-            int64_t gpix;
-            const bool inimg = tile_pixel<TP>(S, tile, p, &gpix);
-            f3 Pp = mk(0.0f, 0.0f, 0.0f), N = mk(0.0f, 0.0f, 0.0f);
-            float ro = c.default_rough;
-            if (inimg) {
-                Pp = ld3(S.pos + 3 * gpix);
-                N = ld3(S.nrm + 3 * gpix);
-                if (S.rough) ro = S.rough[gpix];
-            }
-            const bool sky = !inimg || (N.x == 0.0f && N.y == 0.0f && N.z == 0.0f);
-            const f3 O = add(Pp, mul(N, c.bias));
-            f3 T, B;
-            tangent_frame(N, &T, &B);
-            for (int k = lane; k < R; k += 32) res_hit[k] = 0u;
-            int live = 0;
-            const int rounds = (R + LPP - 1) / LPP;
-            for (int j = 0; j < rounds; j++) {
-                const int kk = j * LPP + lane / TP;
-                const int k = !c.spec_first ? kk : (kk < c.n_spec ? c.n_shadow + c.n_ao + kk : kk - c.n_spec);
-                bool is_live = false;
-                PSlot sl;
-                if (kk < R && !sky) {
-                    const f3 d = gen_dir(c, k, (uint32_t)gpix + S.pix_base, Pp, N, T, B, ro);
-                    const float maxt = kind_maxt(c, k);
-                    const int meta = (p << 4) | (k << 9);
-                    if (!ray_domain_ok(O, d)) {
-                        // no traversal: a miss
-                    } else if (!dir_fast_ok(d)) {
-                        is_live = true;
-                        sl.c01 = 0;
-                        sl.c2m = (meta | kMetaLit) << 16;
-                        sl.a0 = O.x; sl.a1 = O.y; sl.a2 = O.z;
-                        sl.b0 = d.x; sl.b1 = d.y; sl.b2 = d.z;
-                    } else {
-                        DState s;
-                        dda_init(s, O, d, maxt);
-                        // an origin cell outside the bounds ends the ray at the first test (Light.frag:53)
-                        if ((unsigned)s.cx <= ux && (unsigned)s.cy <= uy && (unsigned)s.cz <= uz) {
-                            is_live = true;
-                            const int sg = (s.sx < 0 ? 1 : 0) | (s.sy < 0 ? 2 : 0) | (s.sz < 0 ? 4 : 0);
-                            const uint32_t xs = (uint32_t)(s.cx + 4), ys = (uint32_t)(s.cy + 4), zs = (uint32_t)(s.cz + 4);
-                            sl.c01 = (int)((xs & 3u) | ((xs >> 2) << L.hs[0]) | ((ys & 3u) << 2) | ((ys >> 2) << L.hs[1]) |
-                                           ((zs & 3u) << 4) | ((zs >> 2) << L.hs[2]));
-                            sl.c2m = (meta | sg) << 16;
-                            sl.a0 = s.tx; sl.a1 = s.ty; sl.a2 = s.tz;
-                            sl.b0 = s.tdx; sl.b1 = s.tdy; sl.b2 = s.tdz;
-                        }
-                    }
-                }
-                const unsigned lv = __ballot_sync(0xffffffffu, is_live);
-                if (is_live) slots[live + __popc(lv & lanes_below())] = sl;
-                live += __popc(lv);
-            }
-            __syncwarp();
+        if (t0 >= P.S.ntiles) break;
+        for (int gi = 0; gi < grab && t0 + gi < P.S.ntiles; gi++)
+            lean_tile<TP, KSTEP>(P.S, P.L, t0 + gi, slots, res_t, res_hit, lane);
+    }
+}
 
-            // ------------------------------------------------- B: traversal
-            int base = 0;
-            bool busy = false, retired = false;
-            uint32_t ax = 0, ay = 0, az = 0, kx = 0, ky = 0, kz = 0;
-            float tx = 0.0f, ty = 0.0f, tz = 0.0f, tdx = 0.0f, tdy = 0.0f, tdz = 0.0f, maxt = 0.0f, tot = 0.0f;
-            int n = 0, meta = 0;
-            for (;;) {
-                const bool need = !busy && !retired;
-                const unsigned nm = __ballot_sync(0xffffffffu, need);
-                if (nm) {
-                    if (need) {
-                        const int at = base + __popc(nm & lanes_below());
-                        if (at < live) {
-                            const PSlot sl = slots[at];
-                            meta = (unsigned)sl.c2m >> 16;
-                            const int k = (meta >> 9) & 31;
-                            maxt = kind_maxt(c, k);
-                            if (meta & kMetaLit) {
-                                const Hit h = dda_literal(S.g, mk(sl.a0, sl.a1, sl.a2), mk(sl.b0, sl.b1, sl.b2), maxt);
-                                if (h.flags & VXL_RF_HIT) {
-                                    const int pp = (meta >> 4) & 31;
-                                    res_t[k * TP + pp] = h.t;
-                                    atomicOr(&res_hit[k], 1u << pp);
-                                }
-                            } else {
-                                busy = true;
-                                const uint32_t A = (uint32_t)sl.c01;
-                                ax = A & L.field[0];
-                                ay = A & L.field[1];
-                                az = A & L.field[2];
-                                kx = (meta & 1) ? 0u - L.unit[0] : L.inc[0];
-                                ky = (meta & 2) ? 0u - L.unit[1] : L.inc[1];
-                                kz = (meta & 4) ? 0u - L.unit[2] : L.inc[2];
-                                tx = sl.a0; ty = sl.a1; tz = sl.a2;
-                                tdx = sl.b0; tdy = sl.b1; tdz = sl.b2;
-                                tot = -INFINITY;
-                                n = 0;
-                            }
-                        } else {
-                            retired = true;
-                        }
-                    }
-                    base += __popc(nm);
-                }
-                if (!__any_sync(0xffffffffu, busy) && base >= live) break;
-                if (busy) {
-                    int res = 0;
-                    float ht = 0.0f;
-                    if (__all_sync(__activemask(), n + KSTEP <= 256)) {
-                        const int st = lean_batch<KSTEP>(L.w, ax, ay, az, tx, ty, tz, tdx, tdy, tdz, kx, ky, kz,
-                                                         keep_y, keep_z, one, two27, maxt, tot);
-                        if (st == 1)
-                            res = lean_set_cell(L, ax, ay, az, tx, ty, tz, tot, maxt, &ht) ? 1 : 2;
-                        else if (st == 2)
-                            res = 2;
-                        else {
-                            n += KSTEP;
-                            if (!(tot < maxt)) res = 2;
-                        }
-                    } else {
-                        // the batch may reach the 256-iteration cap: test it, and maxt, at every iteration
-                        for (int it = 0; it < KSTEP; it++) {
-                            if (n >= 256) {
-                                res = 2;
-                                break;
-                            }
-                            res = lean_step(L, ax, ay, az, tx, ty, tz, tdx, tdy, tdz, kx, ky, kz, maxt, tot, &ht);
-                            if (res) break;
-                            n++;
-                            if (!(tot < maxt) || n >= 256) {
-                                res = 2;
-                                break;
-                            }
-                        }
-                    }
-                    if (res) {
-                        if (res == 1) {
-                            const int k = (meta >> 9) & 31, pp = (meta >> 4) & 31;
-                            res_t[k * TP + pp] = ht;
-                            atomicOr(&res_hit[k], 1u << pp);
-                        }
-                        busy = false;
-                    }
-                }
+// many scenes, one counter over all their tiles (work stealing across
+// scenes); tiles are numbered scene after scene, table[i].S.tile_begin ascending
+template <int TP, int KSTEP>
+__global__ void __launch_bounds__(128, VXL_LEAN_MIN_BLOCKS) k_occl_lean_batch(const LeanScene* __restrict__ table,
+                                                                              int nscenes, int64_t total_tiles,
+                                                                              int max_r,
+                                                                              unsigned long long* __restrict__ counter,
+                                                                              int grab) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned char* wbase = smem + warp * pool_bytes(TP, max_r);
+    for (;;) {
+        int64_t t0 = 0;
+        if (lane == 0) t0 = (int64_t)atomicAdd(counter, (unsigned long long)grab);
+        t0 = __shfl_sync(0xffffffffu, t0, 0);
+        if (t0 >= total_tiles) break;
+        for (int gi = 0; gi < grab && t0 + gi < total_tiles; gi++) {
+            const int64_t t = t0 + gi;
+            int lo = 0, hi = nscenes - 1;  // last scene with tile_begin <= t
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (table[mid].S.tile_begin <= t) lo = mid; else hi = mid - 1;
             }
-            __syncwarp();
-
-            // ------------------------------------------------------ C: fold
-            if (lane < TP && inimg) {
-                float sh = 1.0f, ao = 1.0f, vis = 1.0f, sp = 1.0f, st = c.spec_len;
-                if (!sky) {
-                    int k = 0;
-                    if (c.n_shadow > 0) {
-                        sh = ((res_hit[0] >> p) & 1u) ? 0.0f : 1.0f;
-                        k = 1;
-                    }
-                    float acc = 0.0f, v = 0.0f;
-                    for (int j = 0; j < c.n_ao; j++, k++) {
-                        const bool hit = (res_hit[k] >> p) & 1u;
-                        const float t = res_t[k * TP + p];
-                        float tt = hit ? (t < c.ao_len ? t : c.ao_len) : c.ao_len;
-                        float q = tt / c.ao_len;
-                        acc += q * q;
-                        v += hit ? 0.0f : 1.0f;
-                    }
-                    if (c.n_ao > 0) {
-                        ao = acc / (float)c.n_ao;
-                        vis = v / (float)c.n_ao;
-                    }
-                    if (c.n_spec > 0) {
-                        float spa = 0.0f, sta = 0.0f;
-                        for (int j = 0; j < c.n_spec; j++, k++) {
-                            const bool hit = (res_hit[k] >> p) & 1u;
-                            spa += hit ? 0.0f : 1.0f;
-                            sta += hit ? res_t[k * TP + p] : c.spec_len;
-                        }
-                        sp = spa / (float)c.n_spec;
-                        st = sta / (float)c.n_spec;
-                    }
-                }
-                if (S.o_shadow) S.o_shadow[gpix] = sh;
-                if (S.o_ao) S.o_ao[gpix] = ao;
-                if (S.o_vis) S.o_vis[gpix] = vis;
-                if (S.o_spec) S.o_spec[gpix] = sp;
-                if (S.o_spec_t) S.o_spec_t[gpix] = st;
-            }
-            __syncwarp();
+            const LeanScene& P = table[lo];
+            const int R = P.S.c.R;
+            PSlot* slots = reinterpret_cast<PSlot*>(wbase);
+            float* res_t = reinterpret_cast<float*>(wbase + (size_t)TP * R * sizeof(PSlot));
+            uint32_t* res_hit = reinterpret_cast<uint32_t*>(wbase + (size_t)TP * R * (sizeof(PSlot) + sizeof(float)));
+            lean_tile<TP, KSTEP>(P.S, P.L, t - P.S.tile_begin, slots, res_t, res_hit, lane);
         }
     }
 }
@@ -488,6 +528,83 @@ vxl_status launch_trace_occlusion_lean(vxl_ctx* ctx, const vxl_grid* g, const vx
     if (t.tile_px == 8) return launch_lean_k<8>(ctx, P, d_counter, t, s);
     if (t.tile_px == 32) return launch_lean_k<32>(ctx, P, d_counter, t, s);
     return launch_lean_k<16>(ctx, P, d_counter, t, s);
+}
+
+// ------------------------------------------------------------------ batch
+bool lean_batch_supported(const vxl_batch_item* items, int n, const vxl_tuning& tune) {
+    if (tune.leap == 1) return false;
+    for (int i = 0; i < n; i++)
+        if (!items[i].grid->tl_words) return false;
+    return true;
+}
+
+size_t lean_batch_desc_bytes() { return sizeof(LeanScene); }
+
+// the launch shape of a batch: 8-pixel tiles when the 16-pixel pools of its
+// largest ray count would hold the SM below 8 blocks
+vxl_tuning lean_batch_tuning(const vxl_ctx* ctx, const vxl_batch_item* items, int n, const vxl_tuning& tune) {
+    int mr = 1;
+    for (int i = 0; i < n; i++)
+        mr = std::max(mr, items[i].params.n_shadow + items[i].params.n_ao + items[i].params.n_spec);
+    vxl_tuning t = tune;
+    if (t.tile_px == 16 && (pool_bytes(16, mr) * 4 + 1024) * VXL_LEAN_MIN_BLOCKS > (size_t)ctx->smem_per_sm) {
+        t.tile_px = 8;
+        t.tile_w = 8;
+    }
+    return t;
+}
+
+vxl_status lean_batch_build_table(const vxl_batch_item* items, int n, const vxl_tuning& tune, void* h_table,
+                                  int* max_r, int64_t* total_tiles, int64_t* total_rays) {
+    LeanScene* t = (LeanScene*)h_table;
+    int64_t tiles = 0, rays = 0;
+    int mr = 1;
+    for (int i = 0; i < n; i++) {
+        t[i].S = scene_of(items[i].grid, &items[i].gbuf, &items[i].params, &items[i].out, tune);
+        t[i].S.tile_begin = tiles;
+        t[i].L = lean_grid_of(items[i].grid);
+        tiles += t[i].S.ntiles;
+        rays += items[i].gbuf.npix * t[i].S.c.R;
+        mr = std::max(mr, t[i].S.c.R);
+    }
+    *max_r = mr;
+    *total_tiles = tiles;
+    *total_rays = rays;
+    return VXL_OK;
+}
+
+template <int TP, int KSTEP>
+static vxl_status launch_lean_batch_t(vxl_ctx* ctx, const LeanScene* d_table, int n, int max_r, int64_t total_tiles,
+                                      unsigned long long* counter, int grab, cudaStream_t s) {
+    const size_t smem = pool_bytes(TP, max_r) * 4;
+    auto kern = k_occl_lean_batch<TP, KSTEP>;
+    VXL_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    VXL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem));
+    if (per_sm < 1) return fail(VXL_ERR_NOT_SUPPORTED, "batch pool: %zu bytes of shared memory per block", smem);
+    int64_t blocks = (int64_t)ctx->sm_count * per_sm;
+    const int64_t warps_needed = (total_tiles + grab - 1) / grab;
+    if (blocks * 4 > warps_needed) blocks = (warps_needed + 3) / 4;
+    kern<<<(unsigned)blocks, 128, smem, s>>>(d_table, n, total_tiles, max_r, counter, grab);
+    ctx->launches++;
+    VXL_TRY_CUDA(cudaGetLastError());
+    return VXL_OK;
+}
+
+template <int TP>
+static vxl_status launch_lean_batch_k(vxl_ctx* ctx, const LeanScene* d_table, int n, int max_r, int64_t total_tiles,
+                                      unsigned long long* counter, const vxl_tuning& t, cudaStream_t s) {
+    if (t.kstep <= 4) return launch_lean_batch_t<TP, 4>(ctx, d_table, n, max_r, total_tiles, counter, t.grab, s);
+    return launch_lean_batch_t<TP, 8>(ctx, d_table, n, max_r, total_tiles, counter, t.grab, s);
+}
+
+vxl_status launch_lean_batch(vxl_ctx* ctx, void* d_table, int n, int max_r, int64_t total_tiles, const vxl_tuning& t,
+                             unsigned long long* d_counter, cudaStream_t s) {
+    VXL_TRY_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s));
+    const LeanScene* tab = (const LeanScene*)d_table;
+    if (t.tile_px == 8) return launch_lean_batch_k<8>(ctx, tab, n, max_r, total_tiles, d_counter, t, s);
+    if (t.tile_px == 32) return launch_lean_batch_k<32>(ctx, tab, n, max_r, total_tiles, d_counter, t, s);
+    return launch_lean_batch_k<16>(ctx, tab, n, max_r, total_tiles, d_counter, t, s);
 }
 
 }  // namespace vxl

@@ -374,12 +374,24 @@ bool occl_pool_supported(const vxl_grid* g, const vxl_trace_params* p) {
     return R >= 1 && R <= kPoolMaxR && g->nx <= 32760 && g->ny <= 32760 && g->nz <= 32760;
 }
 
+// the exact-step kernels here run 16- or 32-pixel tiles (8-pixel tiles are
+// chosen below for many rays per pixel); an 8-pixel tuning runs as 16
+static vxl_tuning pool_tuning(const vxl_tuning& t) {
+    vxl_tuning r = t;
+    if (r.tile_px == 8) {
+        r.tile_px = 16;
+        if (r.tile_w == 8) r.tile_w = 16;
+    }
+    return r;
+}
+
 vxl_status launch_trace_occlusion_pool(vxl_ctx* ctx, const vxl_grid* g, const vxl_gbuffer* gb,
                                        const vxl_trace_params* p, const vxl_outputs* out,
-                                       unsigned long long* d_counter, const vxl_tuning& tune, cudaStream_t s,
+                                       unsigned long long* d_counter, const vxl_tuning& tune_in, cudaStream_t s,
                                        uint32_t pix_base) {
-    if (occl_lean_supported(g, out, tune))
-        return launch_trace_occlusion_lean(ctx, g, gb, p, out, d_counter, tune, s, pix_base);
+    if (occl_lean_supported(g, out, tune_in))
+        return launch_trace_occlusion_lean(ctx, g, gb, p, out, d_counter, tune_in, s, pix_base);
+    const vxl_tuning tune = pool_tuning(tune_in);
     // Many rays per pixel: the 16-pixel pool's shared memory would hold the SM
     // below the 8 blocks its registers allow, so such frames run 8-pixel tiles
     // (runs of pixels) in the exact-step kernel.
@@ -455,8 +467,9 @@ static vxl_status launch_batch_k(vxl_ctx* ctx, const BatchPlan& b, cudaStream_t 
 
 size_t batch_desc_bytes() { return sizeof(SceneDesc); }
 
-vxl_status batch_build_table(const vxl_batch_item* items, int n, const vxl_tuning& tune, void* h_table, int* max_r,
+vxl_status batch_build_table(const vxl_batch_item* items, int n, const vxl_tuning& tune_in, void* h_table, int* max_r,
                              int64_t* total_tiles, int64_t* total_rays, size_t* max_grid_bytes) {
+    const vxl_tuning tune = pool_tuning(tune_in);
     SceneDesc* t = (SceneDesc*)h_table;
     int64_t tiles = 0, rays = 0;
     int mr = 1;
@@ -476,8 +489,9 @@ vxl_status batch_build_table(const vxl_batch_item* items, int n, const vxl_tunin
     return VXL_OK;
 }
 
-vxl_status launch_batch(vxl_ctx* ctx, void* d_table, int n, int max_r, int64_t total_tiles, const vxl_tuning& tune,
+vxl_status launch_batch(vxl_ctx* ctx, void* d_table, int n, int max_r, int64_t total_tiles, const vxl_tuning& tune_in,
                         unsigned long long* d_counter, size_t max_grid_bytes, cudaStream_t s) {
+    const vxl_tuning tune = pool_tuning(tune_in);
     BatchPlan b{(SceneDesc*)d_table, n, max_r, total_tiles, tune, d_counter, max_grid_bytes > kStepLoadMaxBytes};
     VXL_TRY_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s));
     if (tune.tile_px == 16) return b.cache ? launch_batch_k<16, true>(ctx, b, s) : launch_batch_k<16, false>(ctx, b, s);

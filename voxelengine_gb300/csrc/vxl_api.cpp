@@ -276,7 +276,8 @@ vxl_status vxl_ctx_set_tuning(vxl_ctx* ctx, const vxl_tuning* t) {
     if (!ctx || !t) return fail(VXL_ERR_INVALID_ARG, "ctx_set_tuning: NULL argument");
     vxl_tuning n = ctx->tune;
     if (t->tile_px) {
-        if (t->tile_px != 16 && t->tile_px != 32) return fail(VXL_ERR_INVALID_ARG, "tile_px must be 16 or 32");
+        if (t->tile_px != 8 && t->tile_px != 16 && t->tile_px != 32)
+            return fail(VXL_ERR_INVALID_ARG, "tile_px must be 8, 16 or 32");
         n.tile_px = t->tile_px;
     }
     if (t->kstep) {
@@ -603,6 +604,7 @@ struct vxl_batch {
     int64_t tiles, rays;
     size_t max_grid_bytes;
     vxl_tuning tune;
+    bool lean;  // traced on the grids' trace layouts (k_occl_lean_batch)
     cudaStream_t cap_stream;
     cudaGraph_t graph;
     cudaGraphExec_t exec;
@@ -630,8 +632,16 @@ vxl_status vxl_batch_create(vxl_ctx* ctx, const vxl_batch_item* items, int n, in
     b->ctx = ctx;
     b->n = n;
     b->tune = ctx->tune;
-    std::vector<unsigned char> table((size_t)n * batch_desc_bytes());
-    batch_build_table(items, n, b->tune, table.data(), &b->max_r, &b->tiles, &b->rays, &b->max_grid_bytes);
+    b->lean = lean_batch_supported(items, n, b->tune);
+    std::vector<unsigned char> table;
+    if (b->lean) {
+        b->tune = lean_batch_tuning(ctx, items, n, b->tune);
+        table.resize((size_t)n * lean_batch_desc_bytes());
+        lean_batch_build_table(items, n, b->tune, table.data(), &b->max_r, &b->tiles, &b->rays);
+    } else {
+        table.resize((size_t)n * batch_desc_bytes());
+        batch_build_table(items, n, b->tune, table.data(), &b->max_r, &b->tiles, &b->rays, &b->max_grid_bytes);
+    }
     auto cleanup = [b]() {
         if (b->exec) cudaGraphExecDestroy(b->exec);
         if (b->graph) cudaGraphDestroy(b->graph);
@@ -654,8 +664,10 @@ vxl_status vxl_batch_create(vxl_ctx* ctx, const vxl_batch_item* items, int n, in
             cleanup();
             return cuda_fail(e, "batch_create: begin capture");
         }
-        vxl_status st = launch_batch(ctx, b->d_table, n, b->max_r, b->tiles, b->tune, b->d_counter, b->max_grid_bytes,
-                                     b->cap_stream);
+        vxl_status st = b->lean ? launch_lean_batch(ctx, b->d_table, n, b->max_r, b->tiles, b->tune, b->d_counter,
+                                                    b->cap_stream)
+                                : launch_batch(ctx, b->d_table, n, b->max_r, b->tiles, b->tune, b->d_counter,
+                                               b->max_grid_bytes, b->cap_stream);
         ctx->launches--;  // captured, not run
         e = cudaStreamEndCapture(b->cap_stream, &b->graph);
         if (st != VXL_OK || e != cudaSuccess) {
@@ -681,6 +693,7 @@ vxl_status vxl_batch_run(vxl_batch* b, void* stream) {
         b->ctx->launches++;
         return VXL_OK;
     }
+    if (b->lean) return launch_lean_batch(b->ctx, b->d_table, b->n, b->max_r, b->tiles, b->tune, b->d_counter, s);
     return launch_batch(b->ctx, b->d_table, b->n, b->max_r, b->tiles, b->tune, b->d_counter, b->max_grid_bytes, s);
 }
 

@@ -156,6 +156,15 @@ vxl_status launch_trace_occlusion_lean(vxl_ctx* ctx, const vxl_grid* g, const vx
                                        const vxl_trace_params* p, const vxl_outputs* out,
                                        unsigned long long* d_counter, const vxl_tuning& tune, cudaStream_t s,
                                        uint32_t pix_base);
+// batched occlusion on the trace layouts: every grid of the batch has one and
+// the exact-leap tuning is off (occl_lean.cu)
+bool lean_batch_supported(const vxl_batch_item* items, int n, const vxl_tuning& tune);
+size_t lean_batch_desc_bytes();
+vxl_tuning lean_batch_tuning(const vxl_ctx* ctx, const vxl_batch_item* items, int n, const vxl_tuning& tune);
+vxl_status lean_batch_build_table(const vxl_batch_item* items, int n, const vxl_tuning& tune, void* h_table,
+                                  int* max_r, int64_t* total_tiles, int64_t* total_rays);
+vxl_status launch_lean_batch(vxl_ctx* ctx, void* d_table, int n, int max_r, int64_t total_tiles, const vxl_tuning& t,
+                             unsigned long long* d_counter, cudaStream_t s);
 // the work-queue counter for one persistent launch on stream s (see d_counters)
 vxl_status ctx_take_counter(vxl_ctx* ctx, cudaStream_t s, unsigned long long** out);
 // batched occlusion: scene table built on the host, uploaded once, one launch
