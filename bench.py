@@ -721,9 +721,14 @@ def c4_result(args, steps, warmup, fd_check=True, cpu_baseline=True):
         h = 1e-4
         threads = os.cpu_count() or 1
 
+        # the oracle seeds each pixel's rays with its index: render the whole frame
+        # with the unselected pixels' normals zeroed (they trace nothing)
+        nrm_sel = np.zeros_like(nrm)
+        nrm_sel[sel] = nrm[sel]
+
         def lossv(v, d):
-            return float((oracle.soft_render(vox, pos[sel], nrm[sel], op, perturb_voxel=v, perturb_delta=d,
-                                             threads=threads) * g_sel).sum())
+            return float((oracle.soft_render(vox, pos, nrm_sel, op, perturb_voxel=v, perturb_delta=d,
+                                             threads=threads)[sel] * g_sel).sum())
 
         fd = np.array([(lossv(v, h) - lossv(v, -h)) / (2 * h) for v in pick])
         err = np.abs(got[pick] - fd) / np.maximum(np.abs(fd), 1e-3 * np.abs(fd).max())

@@ -23,6 +23,7 @@
 //  - The 256-iteration cap (Light.frag:75) is tested per batch: a batch that
 //    might reach it runs the iterations with the cap and maxt tests in place.
 #include <algorithm>
+#include <cstring>
 
 #include "occl_common.cuh"
 
@@ -39,7 +40,7 @@ struct LeanGrid {
     int hs[3];                        // shift of each axis's brick index
 };
 
-struct LeanScene {
+struct __align__(16) LeanScene {
     SceneDesc S;
     LeanGrid L;
 };
@@ -423,7 +424,7 @@ __device__ __forceinline__ void lean_tile(const SceneDesc& S, const LeanGrid& L,
 
 // one scene; its descriptor lives in kernel parameter space
 template <int TP, int KSTEP>
-__global__ void __launch_bounds__(128, VXL_LEAN_MIN_BLOCKS) k_occl_lean(const LeanScene P,
+__global__ void __launch_bounds__(128, VXL_LEAN_MIN_BLOCKS) k_occl_lean(const __grid_constant__ LeanScene P,
                                                                         unsigned long long* __restrict__ counter,
                                                                         int grab) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -454,6 +455,12 @@ __global__ void __launch_bounds__(128, VXL_LEAN_MIN_BLOCKS) k_occl_lean_batch(co
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned char* wbase = smem + warp * pool_bytes(TP, max_r);
+    // each warp keeps the descriptor of the scene it works on in shared memory
+    // (after the four pools): it changes only when a warp's tiles move on to
+    // another scene, and the tile loop reads it many times
+    LeanScene* desc = reinterpret_cast<LeanScene*>(smem + 4 * pool_bytes(TP, max_r)) + warp;
+    int cur = -1;
+    int64_t cur_begin = 0, cur_end = 0;
     for (;;) {
         int64_t t0 = 0;
         if (lane == 0) t0 = (int64_t)atomicAdd(counter, (unsigned long long)grab);
@@ -461,12 +468,65 @@ __global__ void __launch_bounds__(128, VXL_LEAN_MIN_BLOCKS) k_occl_lean_batch(co
         if (t0 >= total_tiles) break;
         for (int gi = 0; gi < grab && t0 + gi < total_tiles; gi++) {
             const int64_t t = t0 + gi;
-            int lo = 0, hi = nscenes - 1;  // last scene with tile_begin <= t
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (table[mid].S.tile_begin <= t) lo = mid; else hi = mid - 1;
+            if (t < cur_begin || t >= cur_end) {
+                int lo = 0, hi = nscenes - 1;  // last scene with tile_begin <= t
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (table[mid].S.tile_begin <= t) lo = mid; else hi = mid - 1;
+                }
+                if (lo != cur) {
+                    __syncwarp();
+                    const uint32_t* src = reinterpret_cast<const uint32_t*>(table + lo);
+                    uint32_t* dst = reinterpret_cast<uint32_t*>(desc);
+                    for (int k = lane; k < (int)(sizeof(LeanScene) / 4); k += 32) dst[k] = src[k];
+                    __syncwarp();
+                    cur = lo;
+                }
+                cur_begin = desc->S.tile_begin;
+                cur_end = cur_begin + desc->S.ntiles;
             }
-            const LeanScene& P = table[lo];
+            const int R = desc->S.c.R;
+            PSlot* slots = reinterpret_cast<PSlot*>(wbase);
+            float* res_t = reinterpret_cast<float*>(wbase + (size_t)TP * R * sizeof(PSlot));
+            uint32_t* res_hit = reinterpret_cast<uint32_t*>(wbase + (size_t)TP * R * (sizeof(PSlot) + sizeof(float)));
+            lean_tile<TP, KSTEP>(desc->S, desc->L, t - cur_begin, slots, res_t, res_hit, lane);
+        }
+    }
+}
+
+// A batch of up to kLeanBatchMax scenes passed by value as the kernel's
+// parameters (32 KB of parameter space on this GPU): every warp then reads its
+// scene's constants from the constant bank, as the single-scene kernel does.
+constexpr int kLeanBatchMax = 64;
+struct LeanBatchParams {
+    LeanScene s[kLeanBatchMax];
+};
+static_assert(sizeof(LeanBatchParams) + 64 <= 32764, "the batch table fits the kernel parameter space");
+
+template <int TP, int KSTEP>
+__global__ void __launch_bounds__(128, VXL_LEAN_MIN_BLOCKS) k_occl_lean_batch_p(
+    const __grid_constant__ LeanBatchParams T, int nscenes, int64_t total_tiles, int max_r,
+    unsigned long long* __restrict__ counter, int grab) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned char* wbase = smem + warp * pool_bytes(TP, max_r);
+    int cur = 0;
+    for (;;) {
+        int64_t t0 = 0;
+        if (lane == 0) t0 = (int64_t)atomicAdd(counter, (unsigned long long)grab);
+        t0 = __shfl_sync(0xffffffffu, t0, 0);
+        if (t0 >= total_tiles) break;
+        for (int gi = 0; gi < grab && t0 + gi < total_tiles; gi++) {
+            const int64_t t = t0 + gi;
+            if (t < T.s[cur].S.tile_begin || t >= T.s[cur].S.tile_begin + T.s[cur].S.ntiles) {
+                int lo = 0, hi = nscenes - 1;  // last scene with tile_begin <= t
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (T.s[mid].S.tile_begin <= t) lo = mid; else hi = mid - 1;
+                }
+                cur = lo;
+            }
+            const LeanScene& P = T.s[cur];
             const int R = P.S.c.R;
             PSlot* slots = reinterpret_cast<PSlot*>(wbase);
             float* res_t = reinterpret_cast<float*>(wbase + (size_t)TP * R * sizeof(PSlot));
@@ -576,7 +636,8 @@ vxl_status lean_batch_build_table(const vxl_batch_item* items, int n, const vxl_
 template <int TP, int KSTEP>
 static vxl_status launch_lean_batch_t(vxl_ctx* ctx, const LeanScene* d_table, int n, int max_r, int64_t total_tiles,
                                       unsigned long long* counter, int grab, cudaStream_t s) {
-    const size_t smem = pool_bytes(TP, max_r) * 4;
+    static_assert(sizeof(LeanScene) % 16 == 0, "descriptor copies keep 16-byte alignment");
+    const size_t smem = pool_bytes(TP, max_r) * 4 + 4 * sizeof(LeanScene);
     auto kern = k_occl_lean_batch<TP, KSTEP>;
     VXL_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
@@ -591,20 +652,48 @@ static vxl_status launch_lean_batch_t(vxl_ctx* ctx, const LeanScene* d_table, in
     return VXL_OK;
 }
 
+template <int TP, int KSTEP>
+static vxl_status launch_lean_batch_pt(vxl_ctx* ctx, const LeanBatchParams& T, int n, int max_r, int64_t total_tiles,
+                                       unsigned long long* counter, int grab, cudaStream_t s) {
+    const size_t smem = pool_bytes(TP, max_r) * 4;
+    auto kern = k_occl_lean_batch_p<TP, KSTEP>;
+    VXL_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    VXL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem));
+    if (per_sm < 1) return fail(VXL_ERR_NOT_SUPPORTED, "batch pool: %zu bytes of shared memory per block", smem);
+    int64_t blocks = (int64_t)ctx->sm_count * per_sm;
+    const int64_t warps_needed = (total_tiles + grab - 1) / grab;
+    if (blocks * 4 > warps_needed) blocks = (warps_needed + 3) / 4;
+    kern<<<(unsigned)blocks, 128, smem, s>>>(T, n, total_tiles, max_r, counter, grab);
+    ctx->launches++;
+    VXL_TRY_CUDA(cudaGetLastError());
+    return VXL_OK;
+}
+
 template <int TP>
-static vxl_status launch_lean_batch_k(vxl_ctx* ctx, const LeanScene* d_table, int n, int max_r, int64_t total_tiles,
-                                      unsigned long long* counter, const vxl_tuning& t, cudaStream_t s) {
+static vxl_status launch_lean_batch_k(vxl_ctx* ctx, const LeanScene* d_table, const LeanScene* h_table, int n,
+                                      int max_r, int64_t total_tiles, unsigned long long* counter, const vxl_tuning& t,
+                                      cudaStream_t s) {
+    if (h_table && n <= kLeanBatchMax) {
+        // the table by value (unused entries stay zero and are never read)
+        static thread_local LeanBatchParams T;
+        std::memset(&T, 0, sizeof(T));
+        std::memcpy(T.s, h_table, (size_t)n * sizeof(LeanScene));
+        if (t.kstep <= 4) return launch_lean_batch_pt<TP, 4>(ctx, T, n, max_r, total_tiles, counter, t.grab, s);
+        return launch_lean_batch_pt<TP, 8>(ctx, T, n, max_r, total_tiles, counter, t.grab, s);
+    }
     if (t.kstep <= 4) return launch_lean_batch_t<TP, 4>(ctx, d_table, n, max_r, total_tiles, counter, t.grab, s);
     return launch_lean_batch_t<TP, 8>(ctx, d_table, n, max_r, total_tiles, counter, t.grab, s);
 }
 
-vxl_status launch_lean_batch(vxl_ctx* ctx, void* d_table, int n, int max_r, int64_t total_tiles, const vxl_tuning& t,
-                             unsigned long long* d_counter, cudaStream_t s) {
+vxl_status launch_lean_batch(vxl_ctx* ctx, void* d_table, const void* h_table, int n, int max_r, int64_t total_tiles,
+                             const vxl_tuning& t, unsigned long long* d_counter, cudaStream_t s) {
     VXL_TRY_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s));
     const LeanScene* tab = (const LeanScene*)d_table;
-    if (t.tile_px == 8) return launch_lean_batch_k<8>(ctx, tab, n, max_r, total_tiles, d_counter, t, s);
-    if (t.tile_px == 32) return launch_lean_batch_k<32>(ctx, tab, n, max_r, total_tiles, d_counter, t, s);
-    return launch_lean_batch_k<16>(ctx, tab, n, max_r, total_tiles, d_counter, t, s);
+    const LeanScene* htab = (const LeanScene*)h_table;
+    if (t.tile_px == 8) return launch_lean_batch_k<8>(ctx, tab, htab, n, max_r, total_tiles, d_counter, t, s);
+    if (t.tile_px == 32) return launch_lean_batch_k<32>(ctx, tab, htab, n, max_r, total_tiles, d_counter, t, s);
+    return launch_lean_batch_k<16>(ctx, tab, htab, n, max_r, total_tiles, d_counter, t, s);
 }
 
 }  // namespace vxl

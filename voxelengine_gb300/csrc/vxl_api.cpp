@@ -605,6 +605,7 @@ struct vxl_batch {
     size_t max_grid_bytes;
     vxl_tuning tune;
     bool lean;  // traced on the grids' trace layouts (k_occl_lean_batch)
+    std::vector<unsigned char> h_table;  // host copy of the scene table
     cudaStream_t cap_stream;
     cudaGraph_t graph;
     cudaGraphExec_t exec;
@@ -653,6 +654,7 @@ vxl_status vxl_batch_create(vxl_ctx* ctx, const vxl_batch_item* items, int n, in
     cudaError_t e = cudaMalloc(&b->d_table, table.size());
     if (e == cudaSuccess) e = cudaMalloc(&b->d_counter, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemcpy(b->d_table, table.data(), table.size(), cudaMemcpyHostToDevice);
+    b->h_table = table;
     if (e != cudaSuccess) {
         cleanup();
         return cuda_fail(e, "batch_create: device table");
@@ -664,8 +666,8 @@ vxl_status vxl_batch_create(vxl_ctx* ctx, const vxl_batch_item* items, int n, in
             cleanup();
             return cuda_fail(e, "batch_create: begin capture");
         }
-        vxl_status st = b->lean ? launch_lean_batch(ctx, b->d_table, n, b->max_r, b->tiles, b->tune, b->d_counter,
-                                                    b->cap_stream)
+        vxl_status st = b->lean ? launch_lean_batch(ctx, b->d_table, b->h_table.data(), n, b->max_r, b->tiles, b->tune,
+                                                    b->d_counter, b->cap_stream)
                                 : launch_batch(ctx, b->d_table, n, b->max_r, b->tiles, b->tune, b->d_counter,
                                                b->max_grid_bytes, b->cap_stream);
         ctx->launches--;  // captured, not run
@@ -693,7 +695,9 @@ vxl_status vxl_batch_run(vxl_batch* b, void* stream) {
         b->ctx->launches++;
         return VXL_OK;
     }
-    if (b->lean) return launch_lean_batch(b->ctx, b->d_table, b->n, b->max_r, b->tiles, b->tune, b->d_counter, s);
+    if (b->lean)
+        return launch_lean_batch(b->ctx, b->d_table, b->h_table.data(), b->n, b->max_r, b->tiles, b->tune, b->d_counter,
+                                 s);
     return launch_batch(b->ctx, b->d_table, b->n, b->max_r, b->tiles, b->tune, b->d_counter, b->max_grid_bytes, s);
 }
 

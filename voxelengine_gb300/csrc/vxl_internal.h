@@ -163,8 +163,10 @@ size_t lean_batch_desc_bytes();
 vxl_tuning lean_batch_tuning(const vxl_ctx* ctx, const vxl_batch_item* items, int n, const vxl_tuning& tune);
 vxl_status lean_batch_build_table(const vxl_batch_item* items, int n, const vxl_tuning& tune, void* h_table,
                                   int* max_r, int64_t* total_tiles, int64_t* total_rays);
-vxl_status launch_lean_batch(vxl_ctx* ctx, void* d_table, int n, int max_r, int64_t total_tiles, const vxl_tuning& t,
-                             unsigned long long* d_counter, cudaStream_t s);
+// h_table: the host copy of the table; batches of up to 64 scenes pass it by
+// value as kernel parameters, larger ones read d_table
+vxl_status launch_lean_batch(vxl_ctx* ctx, void* d_table, const void* h_table, int n, int max_r, int64_t total_tiles,
+                             const vxl_tuning& t, unsigned long long* d_counter, cudaStream_t s);
 // the work-queue counter for one persistent launch on stream s (see d_counters)
 vxl_status ctx_take_counter(vxl_ctx* ctx, cudaStream_t s, unsigned long long** out);
 // batched occlusion: scene table built on the host, uploaded once, one launch
