@@ -63,20 +63,22 @@ __device__ __forceinline__ float kind_maxt(const TraceConstsP& c, int k) {
 }
 
 // ray k of a pixel (same generator as k_occlusion / the oracle's occlusion_pixel)
-__device__ __forceinline__ f3 gen_dir(const TraceConstsP& c, int k, uint32_t pix, f3 P, f3 N, f3 T, f3 B, float rough) {
+// hpix = pcg(seed_h + pixel): the per-pixel half of rand01, hoisted by callers
+__device__ __forceinline__ f3 gen_dir(const TraceConstsP& c, int k, uint32_t hpix, f3 P, f3 N, f3 T, f3 B,
+                                      float rough) {
     if (k < c.n_shadow) return c.light;
     if (k < c.n_shadow + c.n_ao) {
         uint32_t j = (uint32_t)(k - c.n_shadow);
-        float u1 = rand01(c.seed_h, pix, 64u + 2u * j);
-        float u2 = rand01(c.seed_h, pix, 65u + 2u * j);
+        float u1 = u01(pcg(hpix + 64u + 2u * j));
+        float u2 = u01(pcg(hpix + 65u + 2u * j));
         return frame_dir(T, B, N, cosine_sample(u1, u2));
     }
     uint32_t j = (uint32_t)(k - c.n_shadow - c.n_ao);
     float a = rough * rough;
     float a2 = a * a;
     f3 V = normalize(sub(c.cam, P));
-    float u1 = rand01(c.seed_h, pix, 2u * j);
-    float u2 = rand01(c.seed_h, pix, 2u * j + 1u);
+    float u1 = u01(pcg(hpix + 2u * j));
+    float u2 = u01(pcg(hpix + 2u * j + 1u));
     float ct = sqrtf((1.0f - u1) / (1.0f + (a2 - 1.0f) * u1));
     float st2 = 1.0f - ct * ct;
     float sn = sqrtf(st2 > 0.0f ? st2 : 0.0f);

@@ -248,6 +248,7 @@ __device__ __forceinline__ void lean_tile(const SceneDesc& S, const LeanGrid& L,
         if (S.rough) ro = S.rough[gpix];
     }
     const bool sky = !inimg || (N.x == 0.0f && N.y == 0.0f && N.z == 0.0f);
+    const uint32_t hpix = pcg(c.seed_h + ((uint32_t)gpix + S.pix_base));  // rand01's per-pixel hash
     const f3 O = add(Pp, mul(N, c.bias));
     f3 T, B;
     tangent_frame(N, &T, &B);
@@ -260,7 +261,7 @@ __device__ __forceinline__ void lean_tile(const SceneDesc& S, const LeanGrid& L,
         bool is_live = false;
         PSlot sl;
         if (kk < R && !sky) {
-            const f3 d = gen_dir(c, k, (uint32_t)gpix + S.pix_base, Pp, N, T, B, ro);
+            const f3 d = gen_dir(c, k, hpix, Pp, N, T, B, ro);
             const float maxt = kind_maxt(c, k);
             const int meta = (p << 4) | (k << 9);
             if (!ray_domain_ok(O, d)) {

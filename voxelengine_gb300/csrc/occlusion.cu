@@ -47,6 +47,7 @@ __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView&
         if (S.rough) ro = S.rough[gpix];
     }
     const bool sky = !inimg || (N.x == 0.0f && N.y == 0.0f && N.z == 0.0f);
+    const uint32_t hpix = pcg(c.seed_h + ((uint32_t)gpix + S.pix_base));  // rand01's per-pixel hash
     const f3 O = add(P, mul(N, c.bias));
     f3 T, B;
     tangent_frame(N, &T, &B);
@@ -61,7 +62,7 @@ __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView&
         bool is_live = false;
         PSlot sl;
         if (kk < R && !sky) {
-            const f3 d = gen_dir(c, k, (uint32_t)gpix + S.pix_base, P, N, T, B, ro);
+            const f3 d = gen_dir(c, k, hpix, P, N, T, B, ro);
             const float maxt = kind_maxt(c, k);
             int meta = (p << 4) | (k << 9);
             Hit h0{0, 0, 0, 0.0f, 0, VXL_RF_EXIT_BOUNDS};

@@ -315,9 +315,10 @@ __device__ __forceinline__ void dda_init(DState& s, f3 o, f3 d, float maxt) {
     s.sx = d.x > 0.0f ? 1 : -1;
     s.sy = d.y > 0.0f ? 1 : -1;
     s.sz = d.z > 0.0f ? 1 : -1;
-    s.tdx = 1.0f / fabsf(d.x);
-    s.tdy = 1.0f / fabsf(d.y);
-    s.tdz = 1.0f / fabsf(d.z);
+    // 1/|d|: the correctly rounded reciprocal, which is what the IEEE division 1/|d| gives
+    s.tdx = __frcp_rn(fabsf(d.x));
+    s.tdy = __frcp_rn(fabsf(d.y));
+    s.tdz = __frcp_rn(fabsf(d.z));
     s.cx = (int)floorf(o.x);
     s.cy = (int)floorf(o.y);
     s.cz = (int)floorf(o.z);
