@@ -118,6 +118,52 @@ __global__ void k_trace_layout(GridView g, TraceLayout t, uint32_t nwords) {
     t.words[i] = w;
 }
 
+// level 1 of the map of empty space: tile t's bit is the OR of the tile
+// map's bits of t and its 26 neighbours
+__global__ void k_clear1(const uint32_t* __restrict__ tmask, uint32_t* __restrict__ out, int tx, int ty, int tz,
+                         uint32_t ntiles, uint32_t nmask) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nmask * 32u) return;
+    bool any = false;
+    if (t < ntiles) {
+        const uint32_t txy = (uint32_t)tx * (uint32_t)ty;
+        const int z = (int)(t / txy), r = (int)(t - (uint32_t)z * txy);
+        const int y = r / tx, x = r - y * tx;
+        for (int dz = -1; dz <= 1 && !any; dz++)
+            for (int dy = -1; dy <= 1 && !any; dy++)
+                for (int dx = -1; dx <= 1 && !any; dx++) {
+                    const int xx = x + dx, yy = y + dy, zz = z + dz;
+                    if (xx < 0 || yy < 0 || zz < 0 || xx >= tx || yy >= ty || zz >= tz) continue;
+                    const uint32_t i = (uint32_t)xx + (uint32_t)yy * (uint32_t)tx + (uint32_t)zz * txy;
+                    any = (tmask[i >> 5] >> (i & 31)) & 1u;
+                }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, any);
+    if ((threadIdx.x & 31) == 0) out[t >> 5] = m;
+}
+
+// level 2: one bit per 8^3 tiles, the OR of their level-1 bits
+__global__ void k_clear2(const uint32_t* __restrict__ c1, uint32_t* __restrict__ out, int tx, int ty, int tz, int sx,
+                         int sy, uint32_t nsuper, uint32_t nwords) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nwords * 32u) return;
+    bool any = false;
+    if (q < nsuper) {
+        const uint32_t sxy = (uint32_t)sx * (uint32_t)sy;
+        const int Z = (int)(q / sxy), r = (int)(q - (uint32_t)Z * sxy);
+        const int Y = r / sx, X = r - Y * sx;
+        const uint32_t txy = (uint32_t)tx * (uint32_t)ty;
+        for (int z = 8 * Z; z < min(8 * Z + 8, tz) && !any; z++)
+            for (int y = 8 * Y; y < min(8 * Y + 8, ty) && !any; y++)
+                for (int x = 8 * X; x < min(8 * X + 8, tx) && !any; x++) {
+                    const uint32_t i = (uint32_t)x + (uint32_t)y * (uint32_t)tx + (uint32_t)z * txy;
+                    any = (c1[i >> 5] >> (i & 31)) & 1u;
+                }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, any);
+    if ((threadIdx.x & 31) == 0) out[q >> 5] = m;
+}
+
 __global__ void k_count(const uint64_t* __restrict__ words, size_t n, unsigned long long* out) {
     unsigned long long c = 0;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -405,6 +451,19 @@ vxl_status launch_build_tile_mask(vxl_grid* g, cudaStream_t s) {
         VXL_TRY_CUDA(launch_trace_layout_view(view_of(g), t, s));
         g->ctx->launches++;
     }
+    return VXL_OK;
+}
+
+vxl_status launch_build_clear_maps(const vxl_grid* g, cudaStream_t s) {
+    if (!g->clear1 || !g->clear2) return fail(VXL_ERR_NOT_SUPPORTED, "clear maps: grid has none");
+    const uint32_t ntiles = (uint32_t)((size_t)g->tx * g->ty * g->tz);
+    k_clear1<<<blocks_for(g->nmask * 32, 256), 256, 0, s>>>(g->tmask, g->clear1, g->tx, g->ty, g->tz, ntiles,
+                                                          (uint32_t)g->nmask);
+    const uint32_t nsuper = (uint32_t)((size_t)g->sx2 * g->sy2 * g->sz2);
+    k_clear2<<<blocks_for(g->nclear2 * 32, 128), 128, 0, s>>>(g->clear1, g->clear2, g->tx, g->ty, g->tz, g->sx2,
+                                                             g->sy2, nsuper, (uint32_t)g->nclear2);
+    g->ctx->launches += 2;
+    VXL_TRY_CUDA(cudaGetLastError());
     return VXL_OK;
 }
 

@@ -16,9 +16,20 @@ struct TraceConstsP {
     uint32_t seed_h;
 };
 
+// The two-level map of empty space (vxl_grid clear1/clear2): level 1, one bit
+// per 8^3 tile, set when the tile or a neighbour has a voxel; level 2, one bit
+// per 64^3 cells (8^3 tiles), set when a level-1 bit in it is. NULL c1: none.
+struct ClearMaps {
+    const uint32_t* c1;
+    const uint32_t* c2;
+    int tx, ty, tz;  // tiles per axis
+    int sx, sy;      // 64^3 regions per x row and per y column
+};
+
 // One scene of a launch: grid, G-buffer, outputs, tiling, ray parameters.
 struct SceneDesc {
     GridView g;
+    ClearMaps cm;
     const float* pos;
     const float* nrm;
     const float* rough;
@@ -109,6 +120,66 @@ __device__ __forceinline__ bool tile_pixel(const SceneDesc& S, int64_t tile, int
     const int64_t x = tx * tw + p % tw, y = ty * th + p / tw;
     *gpix = y * S.width + x;
     return x < S.width && y < S.height;
+}
+
+__device__ __forceinline__ bool map_bit(const uint32_t* m, int x, int y, int z, int nx, int ny) {
+    const uint32_t i = (uint32_t)x + (uint32_t)y * (uint32_t)nx + (uint32_t)z * (uint32_t)nx * (uint32_t)ny;
+    return (__ldg(m + (i >> 5)) >> (i & 31)) & 1u;
+}
+
+// Whether no cell that the DDA state s can still test before its ray ends
+// holds a voxel, proved on the two-level map: the ray is then a miss, whatever
+// ends it (maxt, the bounds or the 256-iteration cap), and needs no more
+// steps. The line is x(T) = fx + sx |d_x| (T - tx) (fx the face crossed at
+// the next x crossing, time tx), and likewise for y and z. From the tile of
+// the current cell, a march steps over clear regions: a whole 64^3 region
+// when its level-2 bit is clear, else an 8^3 tile when its level-1 bit is,
+// else the proof fails. The march covers the line up to time maxt plus two
+// cells (every cell the DDA tests is entered before totalt reaches maxt) or
+// until it leaves the grid's tiles (the DDA would stop at the bounds there).
+// The DDA tests cells the line passes through, and the march's regions are
+// placed from float positions accurate to far less than a tile: the
+// one-tile dilation of level 1 covers both.
+static __device__ __noinline__ bool path_clear(const ClearMaps& M, const DState& s) {
+    const float fx = (float)(s.cx + (s.sx > 0 ? 1 : 0)), fy = (float)(s.cy + (s.sy > 0 ? 1 : 0)),
+                fz = (float)(s.cz + (s.sz > 0 ? 1 : 0));
+    const float vx = (float)s.sx * __frcp_rn(s.tdx), vy = (float)s.sy * __frcp_rn(s.tdy),
+                vz = (float)s.sz * __frcp_rn(s.tdz);  // the direction
+    const float tend = s.maxt + 2.0f * fmaxf(fmaxf(s.tdx, s.tdy), s.tdz);
+    int qx = s.cx >> 3, qy = s.cy >> 3, qz = s.cz >> 3;
+    for (int it = 0; it < 64; it++) {
+        if ((unsigned)qx >= (unsigned)M.tx || (unsigned)qy >= (unsigned)M.ty || (unsigned)qz >= (unsigned)M.tz)
+            return true;
+        int L, x0, y0, z0;  // the clear region: edge in cells and low corner
+        if (!map_bit(M.c2, qx >> 3, qy >> 3, qz >> 3, M.sx, M.sy)) {
+            L = 64;
+            x0 = (qx >> 3) * 64;
+            y0 = (qy >> 3) * 64;
+            z0 = (qz >> 3) * 64;
+        } else if (!map_bit(M.c1, qx, qy, qz, M.tx, M.ty)) {
+            L = 8;
+            x0 = qx * 8;
+            y0 = qy * 8;
+            z0 = qz * 8;
+        } else {
+            return false;
+        }
+        // the times at which the line leaves the region through each far face
+        const float ex = (float)(x0 + (s.sx > 0 ? L : 0)), ey = (float)(y0 + (s.sy > 0 ? L : 0)),
+                    ez = (float)(z0 + (s.sz > 0 ? L : 0));
+        const float Tx = s.tx + (ex - fx) * (float)s.sx * s.tdx;
+        const float Ty = s.ty + (ey - fy) * (float)s.sy * s.tdy;
+        const float Tz = s.tz + (ez - fz) * (float)s.sz * s.tdz;
+        const float T = fminf(fminf(Tx, Ty), Tz);
+        if (!(T == T)) return false;
+        if (T >= tend) return true;
+        // the tile the line enters at T: out of the region along the exit
+        // axes, where the line is along the others
+        qx = (T == Tx ? (s.sx > 0 ? x0 + L : x0 - 1) : __float2int_rd(fx + vx * (T - s.tx))) >> 3;
+        qy = (T == Ty ? (s.sy > 0 ? y0 + L : y0 - 1) : __float2int_rd(fy + vy * (T - s.ty))) >> 3;
+        qz = (T == Tz ? (s.sz > 0 ? z0 + L : z0 - 1) : __float2int_rd(fz + vz * (T - s.tz))) >> 3;
+    }
+    return false;
 }
 
 // host side (occlusion.cu): launch constants and the descriptor of one scene

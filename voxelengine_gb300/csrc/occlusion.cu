@@ -27,7 +27,7 @@ namespace vxl {
 // the bounds or the 256-step cap in them; the batched kernel keeps writing
 // every t, two counters and both tests at every step, which its register
 // allocation prefers
-template <int TP, int KSTEP, bool LEAP, bool RECORDS, bool HIT_T = false, bool CACHE = true>
+template <int TP, int KSTEP, bool LEAP, bool RECORDS, bool HIT_T = false, bool CACHE = true, bool CLEAR = false>
 __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView& g, int64_t tile, PSlot* slots,
                                              float* res_t, uint32_t* res_hit, int lane) {
     constexpr int LPP = 32 / TP;  // lanes per pixel during generation
@@ -109,6 +109,7 @@ __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView&
     int base = 0;
     bool busy = false;  // the lane holds a ray
     bool retired = false;
+    int next_clear = 0;  // CLEAR: step count at which the lane next tries to prove its path empty
     DState s;
     int meta = 0;
     for (;;) {
@@ -148,6 +149,7 @@ __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView&
                         s.leap = (meta & kMetaLeap) != 0;
                         s.wcur = 0xffffffffu;
                         s.word = 0;
+                        next_clear = KSTEP;
                     }
                 } else {
                     retired = true;
@@ -156,6 +158,14 @@ __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView&
             base += __popc(nm);
         }
         if (!__any_sync(0xffffffffu, busy) && base >= live) break;
+        if (CLEAR && busy && s.n >= next_clear) {
+            // a ray whose remaining path is provably empty is a miss: it ends here
+            next_clear = s.n + 4 * KSTEP;
+            // (the cell may be one step out of bounds, which the DDA's next test ends)
+            if ((unsigned)s.cx <= g.ux && (unsigned)s.cy <= g.uy && (unsigned)s.cz <= g.uz &&
+                !map_bit(S.cm.c1, s.cx >> 3, s.cy >> 3, s.cz >> 3, S.cm.tx, S.cm.ty) && path_clear(S.cm, s))
+                busy = false;
+        }
         if (busy) {
             Hit h;
             const int f = dda_run<LEAP, CACHE, HIT_T, HIT_T>(g, s, h, KSTEP);
@@ -221,7 +231,7 @@ __device__ __forceinline__ void process_tile(const SceneDesc& S, const GridView&
 #endif
 
 // one scene; its descriptor lives in kernel parameter space
-template <int TP, int KSTEP, bool LEAP, bool RECORDS, bool CACHE = true>
+template <int TP, int KSTEP, bool LEAP, bool RECORDS, bool CACHE = true, bool CLEAR = false>
 __global__ void __launch_bounds__(128, VXL_POOL_MIN_BLOCKS) k_occl_pool(const SceneDesc S, unsigned long long* __restrict__ counter,
                                                                         int grab) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -237,7 +247,7 @@ __global__ void __launch_bounds__(128, VXL_POOL_MIN_BLOCKS) k_occl_pool(const Sc
         t0 = __shfl_sync(0xffffffffu, t0, 0);
         if (t0 >= S.ntiles) break;
         for (int k = 0; k < grab && t0 + k < S.ntiles; k++)
-            process_tile<TP, KSTEP, LEAP, RECORDS, !RECORDS, CACHE>(S, g, t0 + k, slots, res_t, res_hit, lane);
+            process_tile<TP, KSTEP, LEAP, RECORDS, !RECORDS, CACHE, CLEAR>(S, g, t0 + k, slots, res_t, res_hit, lane);
     }
 }
 
@@ -298,6 +308,7 @@ SceneDesc scene_of(const vxl_grid* g, const vxl_gbuffer* gb, const vxl_trace_par
                           const vxl_tuning& tune) {
     SceneDesc S;
     S.g = view_of(g);
+    S.cm = ClearMaps{g->clear1, g->clear2, g->tx, g->ty, g->tz, g->sx2, g->sy2};
     S.pos = gb->pos;
     S.nrm = gb->nrm;
     S.rough = gb->rough;
@@ -336,11 +347,11 @@ static vxl_status blocks_for_kernel(vxl_ctx* ctx, K kern, size_t smem, int* bloc
     return VXL_OK;
 }
 
-template <int TP, int KSTEP, bool LEAP, bool REC, bool CACHE = true>
+template <int TP, int KSTEP, bool LEAP, bool REC, bool CACHE = true, bool CLEAR = false>
 static vxl_status launch_pool_t(vxl_ctx* ctx, const SceneDesc& S, unsigned long long* counter, int grab,
                                 cudaStream_t s) {
     const size_t smem = pool_bytes(TP, S.c.R) * 4;
-    auto kern = k_occl_pool<TP, KSTEP, LEAP, REC, CACHE>;
+    auto kern = k_occl_pool<TP, KSTEP, LEAP, REC, CACHE, CLEAR>;
     int per_sm = 0;
     VXL_TRY(blocks_for_kernel(ctx, kern, smem, &per_sm));
     int64_t blocks = (int64_t)ctx->sm_count * per_sm;
@@ -352,14 +363,14 @@ static vxl_status launch_pool_t(vxl_ctx* ctx, const SceneDesc& S, unsigned long 
     return VXL_OK;
 }
 
-template <int TP, bool LEAP, bool CACHE>
+template <int TP, bool LEAP, bool CACHE, bool CLEAR = false>
 static vxl_status launch_pool_k(vxl_ctx* ctx, const SceneDesc& S, unsigned long long* counter, const vxl_tuning& t,
                                 cudaStream_t s) {
     switch (t.kstep) {
-        case 1: return launch_pool_t<TP, 1, LEAP, false, CACHE>(ctx, S, counter, t.grab, s);
-        case 2: return launch_pool_t<TP, 2, LEAP, false, CACHE>(ctx, S, counter, t.grab, s);
-        case 4: return launch_pool_t<TP, 4, LEAP, false, CACHE>(ctx, S, counter, t.grab, s);
-        default: return launch_pool_t<TP, 8, LEAP, false, CACHE>(ctx, S, counter, t.grab, s);
+        case 1: return launch_pool_t<TP, 1, LEAP, false, CACHE, CLEAR>(ctx, S, counter, t.grab, s);
+        case 2: return launch_pool_t<TP, 2, LEAP, false, CACHE, CLEAR>(ctx, S, counter, t.grab, s);
+        case 4: return launch_pool_t<TP, 4, LEAP, false, CACHE, CLEAR>(ctx, S, counter, t.grab, s);
+        default: return launch_pool_t<TP, 8, LEAP, false, CACHE, CLEAR>(ctx, S, counter, t.grab, s);
     }
 }
 
@@ -406,6 +417,11 @@ vxl_status launch_trace_occlusion_pool(vxl_ctx* ctx, const vxl_grid* g, const vx
         S8.pix_base = pix_base;
         VXL_TRY_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s));
         const bool cache8 = g->nwords * sizeof(uint64_t) > kStepLoadMaxBytes;
+        if (cache8 && g->clear1 && tune.leap == 3) {
+            // grids beyond L2: rays prove their remaining path empty on the two-level map
+            VXL_TRY(launch_build_clear_maps(g, s));
+            return launch_pool_t<8, 8, false, false, true, true>(ctx, S8, d_counter, t8.grab, s);
+        }
         if (cache8) return launch_pool_t<8, 8, false, false, true>(ctx, S8, d_counter, t8.grab, s);
         return launch_pool_t<8, 8, false, false, false>(ctx, S8, d_counter, t8.grab, s);
     }
@@ -422,6 +438,10 @@ vxl_status launch_trace_occlusion_pool(vxl_ctx* ctx, const vxl_grid* g, const vx
         return launch_pool_k<32, true, true>(ctx, S, d_counter, tune, s);
     }
     const bool cache = g->nwords * sizeof(uint64_t) > kStepLoadMaxBytes;
+    if (cache && g->clear1 && tune.leap == 3 && tune.tile_px == 16) {
+        VXL_TRY(launch_build_clear_maps(g, s));
+        return launch_pool_k<16, false, true, true>(ctx, S, d_counter, tune, s);
+    }
     if (tune.tile_px == 16) {
         if (cache) return launch_pool_k<16, false, true>(ctx, S, d_counter, tune, s);
         return launch_pool_k<16, false, false>(ctx, S, d_counter, tune, s);

@@ -286,7 +286,7 @@ vxl_status vxl_ctx_set_tuning(vxl_ctx* ctx, const vxl_tuning* t) {
         n.kstep = t->kstep;
     }
     if (t->leap) {
-        if (t->leap != 1 && t->leap != 2) return fail(VXL_ERR_INVALID_ARG, "leap must be 1 or 2");
+        if (t->leap != 1 && t->leap != 2 && t->leap != 3) return fail(VXL_ERR_INVALID_ARG, "leap must be 1, 2 or 3");
         n.leap = t->leap;
     }
     if (t->order) {
@@ -340,8 +340,14 @@ vxl_status vxl_grid_create(vxl_ctx* ctx, int nx, int ny, int nz, vxl_grid** out)
     g->nwords = (size_t)nbricks;
     g->nmask = (size_t)((ntiles + 31) / 32);
     trace_layout_dims(g);
+    g->sx2 = (tx + 7) / 8;
+    g->sy2 = (ty + 7) / 8;
+    g->sz2 = (tz + 7) / 8;
+    g->nclear2 = ((size_t)g->sx2 * g->sy2 * g->sz2 + 31) / 32;
     cudaError_t e = cudaMalloc(&g->words, g->nwords * sizeof(uint64_t));
     if (e == cudaSuccess) e = cudaMalloc(&g->tmask, g->nmask * sizeof(uint32_t));
+    if (e == cudaSuccess && !g->tl_nwords) e = cudaMalloc(&g->clear1, g->nmask * sizeof(uint32_t));
+    if (e == cudaSuccess && !g->tl_nwords) e = cudaMalloc(&g->clear2, g->nclear2 * sizeof(uint32_t));
     if (e == cudaSuccess && g->tl_nwords) e = cudaMalloc(&g->tl_words, g->tl_nwords * sizeof(uint64_t));
     if (e == cudaSuccess) e = cudaMemset(g->words, 0, g->nwords * sizeof(uint64_t));
     if (e == cudaSuccess && g->tl_nwords) e = cudaMemset(g->tl_words, 0, g->tl_nwords * sizeof(uint64_t));
@@ -349,6 +355,8 @@ vxl_status vxl_grid_create(vxl_ctx* ctx, int nx, int ny, int nz, vxl_grid** out)
         if (g->words) cudaFree(g->words);
         if (g->tmask) cudaFree(g->tmask);
         if (g->tl_words) cudaFree(g->tl_words);
+        if (g->clear1) cudaFree(g->clear1);
+        if (g->clear2) cudaFree(g->clear2);
         delete g;
         return cuda_fail(e, "grid_create: device allocation");
     }
@@ -361,6 +369,8 @@ vxl_status vxl_grid_create(vxl_ctx* ctx, int nx, int ny, int nz, vxl_grid** out)
         cudaFree(g->words);
         cudaFree(g->tmask);
         if (g->tl_words) cudaFree(g->tl_words);
+        if (g->clear1) cudaFree(g->clear1);
+        if (g->clear2) cudaFree(g->clear2);
         delete g;
         return st;
     }
@@ -374,6 +384,8 @@ vxl_status vxl_grid_destroy(vxl_grid* g) {
     cudaFree(g->words);
     cudaFree(g->tmask);
     if (g->tl_words) cudaFree(g->tl_words);
+    if (g->clear1) cudaFree(g->clear1);
+    if (g->clear2) cudaFree(g->clear2);
     delete g;
     return VXL_OK;
 }

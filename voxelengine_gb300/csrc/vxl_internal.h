@@ -71,6 +71,15 @@ struct vxl_grid {
     uint64_t* tl_words;
     size_t tl_nwords;
     int tl_lbx, tl_lby, tl_bz;
+    // Two-level map of empty space, for grids without a trace layout: level 1
+    // is the tile map dilated by one tile (a tile's bit is set when it or one
+    // of its 26 neighbours has a voxel), level 2 has one bit per 64^3 cells
+    // (8^3 tiles), set when any level-1 bit in it is. Rebuilt from the tile map
+    // by each occlusion call that reads them.
+    uint32_t* clear1;
+    uint32_t* clear2;
+    int sx2, sy2, sz2;  // 64^3 super-tiles per axis
+    size_t nclear2;     // uint32 words of level 2
 };
 
 namespace vxl {
@@ -113,6 +122,8 @@ vxl_status launch_grid_export_r8(const vxl_grid* g, uint8_t* bytes, cudaStream_t
 vxl_status launch_grid_import_palette(vxl_grid* g, const uint8_t* pal, int opaque_min, cudaStream_t s);
 // the tile map and the trace layout, from the words
 vxl_status launch_build_tile_mask(vxl_grid* g, cudaStream_t s);
+// the two-level map of empty space, from the tile map
+vxl_status launch_build_clear_maps(const vxl_grid* g, cudaStream_t s);
 // sets tl_lbx, tl_lby, tl_bz and tl_nwords (0: no trace layout) from the dims
 void trace_layout_dims(vxl_grid* g);
 vxl_status launch_grid_count(const vxl_grid* g, unsigned long long* d_out, cudaStream_t s);
