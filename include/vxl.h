@@ -96,8 +96,9 @@ typedef struct vxl_tuning {
     int32_t tile_px;   /* pixels per warp tile: 8, 16 or 32 (the exact-step and batched kernels run 8 as 16) */
     int32_t kstep;     /* DDA iterations between pool refills: 1, 2, 4 or 8 */
     int32_t leap;      /* empty-space skipping: 1 = cross empty bricks in one step where exact; 2 = none;
-                          3 = on grids without a trace layout (over 64 MiB of brick words), end a ray once its
-                          remaining path is proved empty on the two-level map (dilated 8^3 tiles, 64^3 regions) */
+                          3 = on grids without a trace layout (its bit addresses would not fit in 32 bits: about
+                          1000^3 cells and up), end a ray once its remaining path is proved empty on the two-level
+                          map (dilated 8^3 tiles, 64^3 regions) */
     int32_t order;     /* 1: dispatch spec, shadow, AO; 2: shadow, AO, spec */
     int32_t tile_w;    /* tile shape: pixels per tile row (tile_px = runs of pixels; 4 or 8 = image blocks,
                           used when the G-buffer's width * height == npix) */

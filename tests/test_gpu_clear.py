@@ -1,5 +1,5 @@
-"""The two-level map of empty space (grids too large for the trace layout:
-more than 64 MiB of brick words; tuning leap = 3). A ray whose remaining path is proved empty
+"""The two-level map of empty space (grids too large for the trace layout,
+whose bit addresses must fit in 32 bits; tuning leap = 3). A ray whose remaining path is proved empty
 on the map (dilated 8^3 tiles, 64^3 regions) ends as a miss without more
 steps; every output must still equal the exact stepping of the records pass
 (which never uses the map) over the whole frame, and the oracle on bands of
