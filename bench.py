@@ -297,6 +297,8 @@ def config_dict(wl):
         wl["n_spec"]),
         "grid": [wl["n"]] * 3, "image": [wl["W"], wl["H"]],
         "rays_per_pixel": wl["n_shadow"] + wl["n_ao"] + wl["n_spec"],
+        "storage": "bit-packed occupancy in 4^3 bricks, 8^3 tile map, trace layout; no palette plane (the occlusion "
+                   "outputs read occupancy only, as the ShadowVox image holds)",
         "l2": "flushed between timed steps (256 MiB write outside the per-step events)"}
     if terrain:
         d.update(terrain={"base": wl["n"] / 16.0, "amplitude": 512.0, "octaves": 6}, instances=wl["instances"],
