@@ -30,14 +30,17 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+# storage: "palette4" = bit-packed occupancy with the grid's 4-bit palette plane (seeded indices for the set
+# voxels); "palette8" = the grid imported from a dense uint8 palette-index volume (voxel set where the index is
+# >= 16, as ShadowVoxSystem.cpp:145 sets it); "occupancy" = bit-packed occupancy only
 WORKLOADS = {
     "c2": dict(n=512, W=1920, H=1080, boxes=2000, n_shadow=1, n_ao=8, ao_len=32.0, n_spec=1, spec_len=256.0,
-               shadow_len=100.0, seed=2024),
+               shadow_len=100.0, seed=2024, storage="palette4"),
     "c1": dict(n=256, W=640, H=360, boxes=0, n_shadow=1, n_ao=4, ao_len=16.0, n_spec=0, spec_len=256.0,
-               shadow_len=100.0, seed=2024),
+               shadow_len=100.0, seed=2024, storage="palette8"),
     # stress: 2048^3 terrain (amplitude 512) + 50,000 instances of edge 16-128, 4K frame
     "c5": dict(kind="terrain", n=2048, W=3840, H=2160, boxes=0, instances=50000, n_shadow=1, n_ao=16, ao_len=64.0,
-               n_spec=1, spec_len=256.0, shadow_len=256.0, seed=5),
+               n_spec=1, spec_len=256.0, shadow_len=256.0, seed=5, storage="occupancy"),
 }
 L2_BYTES = 129 * 1024 * 1024
 
@@ -290,6 +293,35 @@ def run_reference(args, wl):
     print(json.dumps(line))
 
 
+STORAGE_TEXT = {
+    "palette4": "bit-packed occupancy in 4^3 bricks with a 4-bit palette plane (seeded indices 1-15 for the set "
+                "voxels; the occlusion traversal reads occupancy only), 8^3 tile map, trace layout",
+    "palette8": "imported from a dense uint8 palette-index volume (voxel set where the index is >= 16) into "
+                "bit-packed occupancy in 4^3 bricks, 8^3 tile map, trace layout",
+    "occupancy": "bit-packed occupancy in 4^3 bricks, 8^3 tile map (the bit addresses exceed 32 bits: no trace "
+                 "layout)",
+}
+
+
+def palette8_volume(G, n, seed):
+    """The dense uint8 palette-index volume behind a grid's occupancy: seeded
+    indices 16-255 where a voxel is set, 0-15 where it is not."""
+    import torch
+
+    import voxelengine_gb300 as V
+
+    r8 = torch.empty((n // 2) ** 3, dtype=torch.uint8, device="cuda")
+    G.export_r8(r8)
+    r8 = r8.view(n // 2, n // 2, n // 2)
+    occ = torch.zeros((n, n, n), dtype=torch.bool, device="cuda")
+    for b in range(8):
+        occ[(b >> 2) & 1::2, (b >> 1) & 1::2, b & 1::2] = ((r8 >> b) & 1).bool()
+    gen = torch.Generator(device="cuda").manual_seed(seed)
+    hi = torch.randint(16, 256, (n, n, n), dtype=torch.uint8, device="cuda", generator=gen)
+    lo = torch.randint(0, 16, (n, n, n), dtype=torch.uint8, device="cuda", generator=gen)
+    return torch.where(occ, hi, lo).contiguous()
+
+
 def config_dict(wl):
     terrain = wl.get("kind") == "terrain"
     d = {"workload": "%s-%d^3-%dx%d-%dshadow+%dao(L%g)+%dspec" % (
@@ -297,8 +329,7 @@ def config_dict(wl):
         wl["n_spec"]),
         "grid": [wl["n"]] * 3, "image": [wl["W"], wl["H"]],
         "rays_per_pixel": wl["n_shadow"] + wl["n_ao"] + wl["n_spec"],
-        "storage": "bit-packed occupancy in 4^3 bricks, 8^3 tile map, trace layout; no palette plane (the occlusion "
-                   "outputs read occupancy only, as the ShadowVox image holds)",
+        "storage": STORAGE_TEXT[wl["storage"]],
         "l2": "flushed between timed steps (256 MiB write outside the per-step events)"}
     if terrain:
         d.update(terrain={"base": wl["n"] / 16.0, "amplitude": 512.0, "octaves": 6}, instances=wl["instances"],
@@ -344,6 +375,14 @@ def run_gpu(args, wl):
         G.scene_noise(wl["seed"], 0.55, 1.0 / 32.0, 8)
         if wl["boxes"]:
             G.scene_boxes(wl["seed"], wl["boxes"], 4, 48)
+        if wl["storage"] == "palette4":
+            G.palette_alloc()
+            G.scene_palette(wl["seed"])
+        elif wl["storage"] == "palette8":
+            vol = palette8_volume(G, n, wl["seed"])
+            G.clear()
+            G.import_palette(vol, opaque_min=16)
+            del vol
         cam, tgt = camera(n)
         pos = torch.empty(npix * 3, dtype=torch.float32, device="cuda")
         nrm = torch.empty_like(pos)
@@ -513,7 +552,7 @@ def c3_result(args, steps, warmup, check=True):
     autotune.apply_cached(ctx, "c3")
     if args.tuning:
         ctx.set_tuning(*[int(x) for x in args.tuning.split(",")])
-    scenes = [S.add_outputs(sc) for sc in S.batch_set(ctx, 64, seed=7)]
+    scenes = [S.add_outputs(sc) for sc in S.batch_set(ctx, 64, seed=7, palette=True)]
     models = S.vox_models(11, 32)
     d_models = [torch.from_numpy(m).cuda() for m in models]
     mdesc = [(d.data_ptr(),) + m.shape[::-1] for m, d in zip(models, d_models)]
@@ -621,7 +660,8 @@ def run_gpu_c3(args):
         "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded scenes, G-buffers and Vox instances)",
         "config": {"workload": "batch-64-scenes", "edges": r.pop("edges"), "pixels": r.pop("pixels"),
-                   "rays_per_pixel": 10, "instances": 10000, "l2": "flushed between timed steps"},
+                   "rays_per_pixel": 10, "instances": 10000, "storage": STORAGE_TEXT["palette4"],
+                   "l2": "flushed between timed steps"},
     }
     line.update({k: v for k, v in r.items() if k not in ("value", "unit", "ms_per_step")})
     print(json.dumps(line))

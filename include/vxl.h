@@ -21,8 +21,9 @@
  *        vxl_light_reflection, vxl_light_point;
  *      - vxl_trace_soft_fwd, vxl_trace_soft_bwd, vxl_volume_build_mips;
  *      - vxl_grid_clear, vxl_grid_build_bricks, vxl_grid_import_r8,
- *        vxl_grid_export_r8, vxl_grid_import_palette;
- *      - vxl_scene_noise, vxl_scene_boxes, vxl_scene_soft, vxl_scene_gbuffer;
+ *        vxl_grid_export_r8, vxl_grid_import_palette, vxl_grid_export_palette;
+ *      - vxl_scene_noise, vxl_scene_boxes, vxl_scene_palette, vxl_scene_soft,
+ *        vxl_scene_gbuffer;
  *      - vxl_batch_run of a batch created with use_graph = 0 (with
  *        use_graph = 1 the batch replays its own graph).
  *    A second group grows a context workspace the first time it sees a
@@ -157,8 +158,21 @@ vxl_status vxl_grid_build_bricks(vxl_grid* grid, void* stream);
 vxl_status vxl_grid_import_r8(vxl_grid* grid, const uint8_t* d_bytes, void* stream);
 vxl_status vxl_grid_export_r8(const vxl_grid* grid, uint8_t* d_bytes, void* stream);
 /* Dense palette-index volume, device uint8 [nz][ny][nx]: voxel set where
- * index >= opaque_min (16 in the reference: ShadowVoxSystem.cpp:145). */
+ * index >= opaque_min (16 in the reference: ShadowVoxSystem.cpp:145). A grid
+ * with a palette plane also keeps the index's low 4 bits of every set voxel
+ * (0 for empty ones). */
 vxl_status vxl_grid_import_palette(vxl_grid* grid, const uint8_t* d_palette, int opaque_min, void* stream);
+/* 4-bit palette plane beside the occupancy bits (4 bits per fine voxel, 32
+ * bytes per 4^3 brick: 64 MiB for 512^3), allocated zeroed on the first call.
+ * No counterpart in the reference, whose ShadowVox image holds occupancy
+ * only: the plane carries a grid's palette indices with it, and the occlusion
+ * traversal never reads it. Written by vxl_grid_import_palette and
+ * vxl_scene_palette, zeroed by vxl_grid_clear; the voxelizer changes
+ * occupancy only. */
+vxl_status vxl_grid_palette_alloc(vxl_grid* grid);
+/* the plane as a dense device uint8 volume [nz][ny][nx] of indices 0..15;
+ * VXL_ERR_NOT_SUPPORTED when the grid has no plane */
+vxl_status vxl_grid_export_palette(const vxl_grid* grid, uint8_t* d_palette, void* stream);
 /* number of set voxels (synchronous) */
 vxl_status vxl_grid_count(const vxl_grid* grid, uint64_t* out, void* stream);
 
@@ -629,6 +643,9 @@ vxl_status vxl_scene_terrain(vxl_ctx* ctx, vxl_grid* grid, uint32_t seed, float 
                              int octaves, float* d_height, void* stream);
 /* OR into the grid: nboxes seeded axis-aligned boxes with edges in [smin, smax] */
 vxl_status vxl_scene_boxes(vxl_ctx* ctx, vxl_grid* grid, uint32_t seed, int nboxes, int smin, int smax, void* stream);
+/* seeded palette plane for the grid's set voxels: index 1 + pcg(seed + pcg(64*brick + bit)) % 15, 0 for empty
+ * voxels (the grid needs a plane: vxl_grid_palette_alloc) */
+vxl_status vxl_scene_palette(vxl_ctx* ctx, vxl_grid* grid, uint32_t seed, void* stream);
 /* primary-visibility G-buffer from a pinhole camera (entry-face DDA):
  * device pos/nrm float[W*H][3], rough float[W*H] */
 vxl_status vxl_scene_gbuffer(vxl_ctx* ctx, const vxl_grid* grid, const float cam[3], const float target[3],

@@ -36,6 +36,7 @@ EXPORTED = [
     "vxl_abi_version", "vxl_last_error_string", "vxl_status_string", "vxl_ctx_create", "vxl_ctx_destroy",
     "vxl_ctx_launch_count", "vxl_ctx_set_tuning", "vxl_ctx_get_tuning", "vxl_grid_create", "vxl_grid_destroy", "vxl_grid_describe", "vxl_grid_clear",
     "vxl_grid_build_bricks", "vxl_grid_import_r8", "vxl_grid_export_r8", "vxl_grid_import_palette",
+    "vxl_grid_palette_alloc", "vxl_grid_export_palette", "vxl_scene_palette",
     "vxl_grid_count", "vxl_trace_rays", "vxl_trace_occlusion", "vxl_trace_occlusion_host",
     "vxl_trace_occlusion_from_depth", "vxl_batch_create",
     "vxl_batch_run", "vxl_batch_destroy", "vxl_batch_info", "vxl_light_ambient",
@@ -186,6 +187,9 @@ def lib():
         L.vxl_grid_import_r8.argtypes = [vp, vp, vp]
         L.vxl_grid_export_r8.argtypes = [vp, vp, vp]
         L.vxl_grid_import_palette.argtypes = [vp, vp, C.c_int, vp]
+        L.vxl_grid_palette_alloc.argtypes = [vp]
+        L.vxl_grid_export_palette.argtypes = [vp, vp, vp]
+        L.vxl_scene_palette.argtypes = [vp, vp, C.c_uint32, vp]
         L.vxl_grid_count.argtypes = [vp, C.POINTER(C.c_uint64), vp]
         L.vxl_trace_rays.argtypes = [vp, vp, vp, i64, C.c_int, vp, vp]
         L.vxl_trace_occlusion.argtypes = [vp, vp, C.POINTER(GBuffer), C.POINTER(TraceParams), C.POINTER(Outputs), vp]
@@ -348,6 +352,17 @@ class Grid:
 
     def import_palette(self, d_pal, opaque_min=16, stream=None):
         check(lib().vxl_grid_import_palette(self._h, _ptr(d_pal), opaque_min, _stream(stream)))
+
+    def palette_alloc(self):
+        """Give the grid its 4-bit palette plane (zeroed; no-op if present)."""
+        check(lib().vxl_grid_palette_alloc(self._h))
+
+    def export_palette(self, d_out, stream=None):
+        """The palette plane as a dense device uint8 volume [nz][ny][nx]."""
+        check(lib().vxl_grid_export_palette(self._h, _ptr(d_out), _stream(stream)))
+
+    def scene_palette(self, seed, stream=None):
+        check(lib().vxl_scene_palette(self.ctx.handle, self._h, seed, _stream(stream)))
 
     def count(self, stream=None) -> int:
         n = C.c_uint64()

@@ -56,22 +56,59 @@ __global__ void k_export_r8(GridView g, uint8_t* __restrict__ bytes, uint32_t nb
 }
 
 // dense palette volume [nz][ny][nx] -> bits (index >= opaque_min)
-__global__ void k_import_palette(GridView g, uint64_t* words, const uint8_t* __restrict__ pal, int opaque_min,
-                                 uint32_t nwords) {
+// pal4 (optional): the grid's 4-bit palette plane, four uint64 per brick
+// (word z of a brick holds layer z, nibble x + 4y): the index's low 4 bits for
+// set voxels, 0 for empty ones.
+__global__ void k_import_palette(GridView g, uint64_t* words, uint64_t* pal4, const uint8_t* __restrict__ pal,
+                                 int opaque_min, uint32_t nwords) {
     uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nwords) return;
     int x0, y0, z0;
     word_origin(g, w, &x0, &y0, &z0);
     uint64_t out = 0;
-    for (int lz = 0; lz < 4; lz++)
+    for (int lz = 0; lz < 4; lz++) {
+        uint64_t layer = 0;
         for (int ly = 0; ly < 4; ly++)
             for (int lx = 0; lx < 4; lx++) {
                 int x = x0 + lx, y = y0 + ly, z = z0 + lz;
                 if (x >= g.nx || y >= g.ny || z >= g.nz) continue;
-                if (pal[(size_t)x + (size_t)y * g.nx + (size_t)z * g.nx * g.ny] >= opaque_min)
+                const uint8_t v = pal[(size_t)x + (size_t)y * g.nx + (size_t)z * g.nx * g.ny];
+                if (v >= opaque_min) {
                     out |= 1ull << (lx | (ly << 2) | (lz << 4));
+                    layer |= (uint64_t)(v & 15u) << (4 * (lx | (ly << 2)));
+                }
             }
+        if (pal4) pal4[4 * (size_t)w + lz] = layer;
+    }
     words[w] = out;
+}
+
+// the palette plane as a dense uint8 volume [nz][ny][nx] (one thread per voxel)
+__global__ void k_export_palette(GridView g, const uint64_t* __restrict__ pal4, uint8_t* out, uint64_t n) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint64_t nxy = (uint64_t)g.nx * g.ny;
+    const int z = (int)(i / nxy), r = (int)(i - (uint64_t)z * nxy);
+    const int y = r / g.nx, x = r - y * g.nx;
+    const uint64_t layer = pal4[4 * (size_t)word_index(g, x, y, z) + (z & 3)];
+    out[i] = (uint8_t)((layer >> (4 * ((x & 3) | ((y & 3) << 2)))) & 15u);
+}
+
+// seeded palette indices for the set voxels (synthetic scenes): 1 + hash % 15
+__global__ void k_scene_palette(GridView g, uint64_t* pal4, uint32_t seed, uint32_t nwords) {
+    const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nwords) return;
+    const uint64_t occ = g.words[w];
+    for (int lz = 0; lz < 4; lz++) {
+        uint64_t layer = 0;
+        for (int b = 0; b < 16; b++) {
+            if ((occ >> (b + 16 * lz)) & 1ull) {
+                const uint32_t h = pcg(seed + pcg(w * 64u + (uint32_t)(b + 16 * lz)));
+                layer |= (uint64_t)(1u + h % 15u) << (4 * b);
+            }
+        }
+        pal4[4 * (size_t)w + lz] = layer;
+    }
 }
 
 // one bit per 8^3 tile: any of its 2x2x2 bricks non-zero
@@ -408,10 +445,26 @@ vxl_status launch_grid_export_r8(const vxl_grid* g, uint8_t* bytes, cudaStream_t
 
 vxl_status launch_grid_import_palette(vxl_grid* g, const uint8_t* pal, int opaque_min, cudaStream_t s) {
     GridView v = view_of(g);
-    k_import_palette<<<blocks_for(g->nwords, 128), 128, 0, s>>>(v, g->words, pal, opaque_min, (uint32_t)g->nwords);
+    k_import_palette<<<blocks_for(g->nwords, 128), 128, 0, s>>>(v, g->words, g->pal4, pal, opaque_min,
+                                                                 (uint32_t)g->nwords);
     g->ctx->launches++;
     VXL_TRY_CUDA(cudaGetLastError());
     return launch_build_tile_mask(g, s);
+}
+
+vxl_status launch_grid_export_palette(const vxl_grid* g, uint8_t* out, cudaStream_t s) {
+    const uint64_t n = (uint64_t)g->nx * g->ny * g->nz;
+    k_export_palette<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(view_of(g), g->pal4, out, n);
+    g->ctx->launches++;
+    VXL_TRY_CUDA(cudaGetLastError());
+    return VXL_OK;
+}
+
+vxl_status launch_scene_palette(vxl_grid* g, uint32_t seed, cudaStream_t s) {
+    k_scene_palette<<<blocks_for(g->nwords, 128), 128, 0, s>>>(view_of(g), g->pal4, seed, (uint32_t)g->nwords);
+    g->ctx->launches++;
+    VXL_TRY_CUDA(cudaGetLastError());
+    return VXL_OK;
 }
 
 void trace_layout_dims(vxl_grid* g) {

@@ -386,6 +386,7 @@ vxl_status vxl_grid_destroy(vxl_grid* g) {
     if (g->tl_words) cudaFree(g->tl_words);
     if (g->clear1) cudaFree(g->clear1);
     if (g->clear2) cudaFree(g->clear2);
+    if (g->pal4) cudaFree(g->pal4);
     delete g;
     return VXL_OK;
 }
@@ -418,6 +419,7 @@ vxl_status vxl_grid_clear(vxl_grid* g, void* stream) {
     if (!grid_ok(g)) return fail(VXL_ERR_INVALID_ARG, "grid_clear: bad grid");
     VXL_TRY(set_device(g->ctx));
     VXL_TRY_CUDA(cudaMemsetAsync(g->words, 0, g->nwords * sizeof(uint64_t), (cudaStream_t)stream));
+    if (g->pal4) VXL_TRY_CUDA(cudaMemsetAsync(g->pal4, 0, 4 * g->nwords * sizeof(uint64_t), (cudaStream_t)stream));
     return launch_build_tile_mask(g, (cudaStream_t)stream);
 }
 
@@ -444,6 +446,29 @@ vxl_status vxl_grid_import_palette(vxl_grid* g, const uint8_t* d_palette, int op
     if (opaque_min < 0 || opaque_min > 256) return fail(VXL_ERR_INVALID_ARG, "opaque_min out of [0,256]");
     VXL_TRY(set_device(g->ctx));
     return launch_grid_import_palette(g, d_palette, opaque_min, (cudaStream_t)stream);
+}
+
+vxl_status vxl_grid_palette_alloc(vxl_grid* g) {
+    if (!grid_ok(g)) return fail(VXL_ERR_INVALID_ARG, "grid_palette_alloc: bad grid");
+    if (g->pal4) return VXL_OK;
+    VXL_TRY(set_device(g->ctx));
+    const size_t bytes = 4 * g->nwords * sizeof(uint64_t);
+    uint64_t* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e == cudaSuccess) e = cudaMemset(p, 0, bytes);
+    if (e != cudaSuccess) {
+        if (p) cudaFree(p);
+        return cuda_fail(e, "grid_palette_alloc: device allocation");
+    }
+    g->pal4 = p;
+    return VXL_OK;
+}
+
+vxl_status vxl_grid_export_palette(const vxl_grid* g, uint8_t* d_out, void* stream) {
+    if (!grid_ok(g) || !d_out) return fail(VXL_ERR_INVALID_ARG, "grid_export_palette: NULL argument");
+    if (!g->pal4) return fail(VXL_ERR_NOT_SUPPORTED, "grid_export_palette: the grid has no palette plane");
+    VXL_TRY(set_device(g->ctx));
+    return launch_grid_export_palette(g, d_out, (cudaStream_t)stream);
 }
 
 vxl_status vxl_grid_count(const vxl_grid* g, uint64_t* out, void* stream) {
@@ -1025,6 +1050,13 @@ vxl_status vxl_scene_terrain(vxl_ctx* ctx, vxl_grid* g, uint32_t seed, float bas
         return fail(VXL_ERR_INVALID_ARG, "scene_terrain: bad argument");
     VXL_TRY(set_device(ctx));
     return launch_scene_terrain(g, seed, base, amplitude, freq, octaves, d_height, (cudaStream_t)stream);
+}
+
+vxl_status vxl_scene_palette(vxl_ctx* ctx, vxl_grid* g, uint32_t seed, void* stream) {
+    if (!ctx || !grid_ok(g)) return fail(VXL_ERR_INVALID_ARG, "scene_palette: bad argument");
+    if (!g->pal4) return fail(VXL_ERR_NOT_SUPPORTED, "scene_palette: the grid has no palette plane");
+    VXL_TRY(set_device(ctx));
+    return launch_scene_palette(g, seed, (cudaStream_t)stream);
 }
 
 vxl_status vxl_scene_boxes(vxl_ctx* ctx, vxl_grid* g, uint32_t seed, int nboxes, int smin, int smax, void* stream) {

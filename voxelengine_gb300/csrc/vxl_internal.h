@@ -80,6 +80,10 @@ struct vxl_grid {
     uint32_t* clear2;
     int sx2, sy2, sz2;  // 64^3 super-tiles per axis
     size_t nclear2;     // uint32 words of level 2
+    // 4-bit palette plane (vxl_grid_palette_alloc), 4 * nwords uint64, or
+    // NULL: word 4b + z of brick b holds its layer z, nibble x + 4y. The
+    // traversal does not read it.
+    uint64_t* pal4;
 };
 
 namespace vxl {
@@ -120,6 +124,8 @@ struct DevModel {
 vxl_status launch_grid_import_r8(vxl_grid* g, const uint8_t* bytes, cudaStream_t s);
 vxl_status launch_grid_export_r8(const vxl_grid* g, uint8_t* bytes, cudaStream_t s);
 vxl_status launch_grid_import_palette(vxl_grid* g, const uint8_t* pal, int opaque_min, cudaStream_t s);
+vxl_status launch_grid_export_palette(const vxl_grid* g, uint8_t* out, cudaStream_t s);
+vxl_status launch_scene_palette(vxl_grid* g, uint32_t seed, cudaStream_t s);
 // the tile map and the trace layout, from the words
 vxl_status launch_build_tile_mask(vxl_grid* g, cudaStream_t s);
 // the two-level map of empty space, from the tile map

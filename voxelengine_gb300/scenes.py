@@ -75,13 +75,18 @@ def instance_matrix(rng, n, model_shape):
     return np.ascontiguousarray(m.T.astype(np.float32)).reshape(16)
 
 
-def make_scene(ctx, n, W, H, seed, thresh=0.55, boxes=0, params=None, device_tensors=True):
+def make_scene(ctx, n, W, H, seed, thresh=0.55, boxes=0, params=None, device_tensors=True, palette=False):
+    """palette: give the grid its 4-bit palette plane with seeded indices for
+    the set voxels (vxl_scene_palette); the traversal does not read it."""
     import torch
 
     G = V.Grid(ctx, n, n, n)
     G.scene_noise(seed, thresh, 1.0 / 32.0, 8)
     if boxes:
         G.scene_boxes(seed, boxes, 4, 48)
+    if palette:
+        G.palette_alloc()
+        G.scene_palette(seed)
     cam, tgt = camera(n)
     npix = W * H
     pos = torch.empty(npix * 3, dtype=torch.float32, device="cuda")
@@ -110,7 +115,7 @@ def make_soft_scene(ctx, n, W, H, seed, albedo_seed=1, thresh=0.55, sharpness=8.
 
 
 def batch_set(ctx, count=64, seed=7, edge_range=(64, 512), rays_range=(64 * 1024, 2 * 1024 * 1024),
-              thresh_range=(0.45, 0.65), rays_per_pixel=10):
+              thresh_range=(0.45, 0.65), rays_per_pixel=10, palette=False):
     """The uneven scene mix: edges log-uniform in edge_range (even), noise
     threshold uniform in thresh_range, rays per scene log-uniform in rays_range."""
     rng = np.random.default_rng(seed)
@@ -120,7 +125,7 @@ def batch_set(ctx, count=64, seed=7, edge_range=(64, 512), rays_range=(64 * 1024
         rays = math.exp(rng.uniform(math.log(rays_range[0]), math.log(rays_range[1])))
         W, H = image_for_pixels(rays / rays_per_pixel)
         thresh = float(rng.uniform(*thresh_range))
-        scenes.append(make_scene(ctx, n, W, H, seed * 1000 + i, thresh=thresh))
+        scenes.append(make_scene(ctx, n, W, H, seed * 1000 + i, thresh=thresh, palette=palette))
     return scenes
 
 
