@@ -298,8 +298,8 @@ STORAGE_TEXT = {
                 "voxels; the occlusion traversal reads occupancy only), 8^3 tile map, trace layout",
     "palette8": "imported from a dense uint8 palette-index volume (voxel set where the index is >= 16) into "
                 "bit-packed occupancy in 4^3 bricks, 8^3 tile map, trace layout",
-    "occupancy": "bit-packed occupancy in 4^3 bricks, 8^3 tile map (the bit addresses exceed 32 bits: no trace "
-                 "layout)",
+    "occupancy": "bit-packed occupancy in 4^3 bricks, 8^3 tile map, wide trace layout (bit addresses of 33-37 "
+                 "bits: the z term in 64 bits)",
 }
 
 

@@ -125,8 +125,9 @@ vxl_status vxl_ctx_get_tuning(const vxl_ctx* ctx, vxl_tuning* out);
  * (Light.frag:53 tests up to 2S+1 inclusive) and 1 on the border just
  * outside those bounds (a coordinate equal to -1 or n+2). The traversal then
  * needs no bounds test: the first cell outside the bounds reads as set, and
- * is reported as the bounds exit. Present when every bit address fits in 32
- * bits (trace_words != NULL); rebuilt with the tile map. */
+ * is reported as the bounds exit. Present when every bit address fits in 37
+ * bits (trace_words != NULL; up to about 2048^3 cells), trace_wide = 1 when
+ * they need more than 32; rebuilt with the tile map. */
 typedef struct vxl_grid_desc {
     int32_t nx, ny, nz;        /* fine dimensions */
     int32_t bx, by, bz;        /* 4^3 bricks per axis, padding included */
@@ -138,7 +139,7 @@ typedef struct vxl_grid_desc {
     uint64_t* trace_words;     /* device: the trace layout, or NULL */
     size_t trace_words_bytes;
     int32_t trace_lbx, trace_lby, trace_bz;
-    int32_t pad;
+    int32_t trace_wide;        /* 1: bit addresses above 32 bits (see above) */
 } vxl_grid_desc;
 
 vxl_status vxl_grid_create(vxl_ctx* ctx, int nx, int ny, int nz, vxl_grid** out);

@@ -62,7 +62,7 @@ class GridDesc(C.Structure):
                 ("bz", C.c_int32), ("tx", C.c_int32), ("ty", C.c_int32), ("tz", C.c_int32), ("words", C.c_void_p),
                 ("words_bytes", C.c_size_t), ("tile_mask", C.c_void_p), ("tile_mask_bytes", C.c_size_t),
                 ("trace_words", C.c_void_p), ("trace_words_bytes", C.c_size_t), ("trace_lbx", C.c_int32),
-                ("trace_lby", C.c_int32), ("trace_bz", C.c_int32), ("pad", C.c_int32)]
+                ("trace_lby", C.c_int32), ("trace_bz", C.c_int32), ("trace_wide", C.c_int32)]
 
 
 class GBuffer(C.Structure):

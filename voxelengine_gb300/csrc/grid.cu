@@ -479,11 +479,16 @@ void trace_layout_dims(vxl_grid* g) {
     g->tl_lby = lg(cy);
     g->tl_bz = cz;
     const int sh = 6 + g->tl_lbx + g->tl_lby;
-    // every bit address must fit in 32 bits
-    if (sh >= 32 || ((unsigned long long)cz << sh) > (1ull << 32)) {
+    // every bit address fits in 32 bits (the x and y terms always must), or in
+    // 37 bits with the z term's brick index above bit 31 (wide: 32-bit word
+    // indices, kept below 2^32 - 1)
+    const unsigned long long bits = (unsigned long long)cz << sh;
+    g->tl_wide = 0;
+    if (sh >= 32 || bits >= (1ull << 37)) {
         g->tl_nwords = 0;
         return;
     }
+    g->tl_wide = bits > (1ull << 32) ? 1 : 0;
     g->tl_nwords = (size_t)cz << (g->tl_lbx + g->tl_lby);
 }
 

@@ -591,8 +591,445 @@ static vxl_status launch_lean_k(vxl_ctx* ctx, const LeanScene& P, unsigned long 
     }
 }
 
+// ------------------------------------------------------ wide trace layout
+// Grids whose bit addresses need 33 to 37 bits (about 1300^3 to 2048^3
+// cells): the x and y terms stay 32-bit, the z term is 64-bit (its brick
+// index lies above bit 31), and a cell's 32-bit word index is the 64-bit
+// address >> 5. Such a grid does not stay in L1 the way a 512^3 one does, so
+// each ray keeps the word it last read and loads only when its word index
+// changes (a 4x4x2 half-brick: about every second step).
+struct LeanGridW {
+    const uint32_t* __restrict__ w;
+    uint32_t field[2], keep[2], inc[2], unit[2], lo[2], span[2];
+    uint64_t fieldz, keepz, incz, unitz, loz, spanz;
+    uint32_t one;
+    int hs[3];
+};
+
+struct __align__(16) LeanSceneW {
+    SceneDesc S;
+    LeanGridW L;
+};
+
+static LeanGridW lean_grid_w_of(const vxl_grid* g) {
+    LeanGridW L;
+    L.w = reinterpret_cast<const uint32_t*>(g->tl_words);
+    const int n[3] = {g->nx, g->ny, g->nz};
+    for (int a = 0; a < 2; a++) {
+        const AxisCode c = axis_code(a, g->tl_lbx, g->tl_lby);
+        L.field[a] = c.field;
+        L.keep[a] = c.keep;
+        L.inc[a] = c.inc;
+        L.unit[a] = c.unit;
+        L.hs[a] = c.hi_shift;
+        L.lo[a] = axis_term(c, 4);
+        L.span[a] = axis_term(c, n[a] + 5) - L.lo[a];
+    }
+    // z: bits 4-5 and the brick index from bit 6 + lbx + lby up (64-bit)
+    const int hz = 6 + g->tl_lbx + g->tl_lby;
+    L.hs[2] = hz;
+    const uint64_t gap = ((1ull << hz) - 1ull) & ~((4ull << 4) - 1ull);
+    L.fieldz = (3ull << 4) | ~((1ull << hz) - 1ull);
+    L.keepz = ~gap;
+    L.unitz = 1ull << 4;
+    L.incz = gap + L.unitz;
+    auto zterm = [&](int v) { return ((uint64_t)(v & 3) << 4) | ((uint64_t)(v >> 2) << hz); };
+    L.loz = zterm(4);
+    L.spanz = zterm(n[2] + 5) - L.loz;
+    L.one = 1u;
+    return L;
+}
+
+// one iteration of Light.frag:50-75 on the wide layout with the word cache
+// (wc: index of the cached word wd); as lean_step
+__device__ __forceinline__ int lean_step_w(const LeanGridW& L, uint32_t& ax, uint32_t& ay, uint64_t& az, float& tx,
+                                           float& ty, float& tz, float tdx, float tdy, float tdz, uint32_t kx,
+                                           uint32_t ky, uint64_t kz, float maxt, float& tot, float* ht, uint32_t& wc,
+                                           uint32_t& wd) {
+    const uint64_t A = (uint64_t)(ax + ay) + az;
+    const uint32_t wi = (uint32_t)(A >> 5);
+    if (wi != wc) {
+        wc = wi;
+        wd = __ldg(L.w + wi);
+    }
+    const float m = fminf(fminf(tx, ty), tz);
+    const bool bx = tx == m, by = ty == m, bz = tz == m;
+    const bool tie = (bx && (by || bz)) || (by && bz);
+    if (__funnelshift_r(wd, wd, (uint32_t)A) & 1u) {
+        if (!(tot < maxt)) return 2;
+        if (ax - L.lo[0] > L.span[0] || ay - L.lo[1] > L.span[1] || az - L.loz > L.spanz) return 2;
+        float best = m + 0.0f;
+        if (tie) {
+            best = (bx ? tx : 0.0f) + (by ? ty : 0.0f);
+            best = best + (bz ? tz : 0.0f);
+        }
+        *ht = best;
+        return 1;
+    }
+    float best = m;
+    if (tie) {
+        best = (bx ? tx : 0.0f) + (by ? ty : 0.0f);
+        best = best + (bz ? tz : 0.0f);
+        if (!(best < maxt)) return 2;
+    }
+    if (bx) {
+        ax = (ax + kx) & L.keep[0];
+        tx = tx + tdx;
+    }
+    if (by) {
+        ay = (ay + ky) & L.keep[1];
+        ty = ty + tdy;
+    }
+    if (bz) {
+        az = (az + kz) & L.keepz;
+        tz = tz + tdz;
+    }
+    tot = best;
+    return 0;
+}
+
+__device__ __forceinline__ bool lean_set_cell_w(const LeanGridW& L, uint32_t ax, uint32_t ay, uint64_t az, float tx,
+                                                float ty, float tz, float tot, float maxt, float* t) {
+    if (!(tot < maxt)) return false;
+    if (ax - L.lo[0] > L.span[0] || ay - L.lo[1] > L.span[1] || az - L.loz > L.spanz) return false;
+    const float m = fminf(fminf(tx, ty), tz);
+    const bool bx = tx == m, by = ty == m, bz = tz == m;
+    float best = m + 0.0f;
+    if ((bx && (by || bz)) || (by && bz)) {
+        best = (bx ? tx : 0.0f) + (by ? ty : 0.0f);
+        best = best + (bz ? tz : 0.0f);
+    }
+    *t = best;
+    return true;
+}
+
+// The hot form on the wide layout: the iteration of VXL_LEAN_IT with the x
+// and y adds as multiply-adds by 1, the z term's add and mask in 64 bits, the
+// word index as a funnel shift of the address's two halves, and the load only
+// when that index differs from the cached one.
+#define VXL_LEANW_IT(i)                       \
+    "mov.b64 {zl, zh}, %2;\n\t"               \
+    "mad.lo.u32 a, %0, %21, %1;\n\t"          \
+    "add.u32 a, a, zl;\n\t"                   \
+    "shf.r.clamp.b32 s, a, zh, 5;\n\t"        \
+    "setp.ne.u32 pw, s, %8;\n\t"              \
+    "@pw mad.wide.u32 ad, s, 4, %18;\n\t"     \
+    "@pw ld.global.nc.u32 %9, [ad];\n\t"      \
+    "@pw mov.u32 %8, s;\n\t"                  \
+    "min.f32 m, %3, %4;\n\t"                  \
+    "min.f32 m, m, %5;\n\t"                   \
+    "setp.eq.f32 px, %3, m;\n\t"              \
+    "setp.eq.f32 py, %4, m;\n\t"              \
+    "setp.eq.f32 pz, %5, m;\n\t"              \
+    "shf.r.wrap.b32 s, %9, %9, a;\n\t"        \
+    "and.b32 s, s, 1;\n\t"                    \
+    "setp.ne.u32 pb, s, 0;\n\t"               \
+    "@pb bra VXL_WSET;\n\t"                   \
+    "@px mad.lo.u32 %0, %13, %21, %0;\n\t"    \
+    "@py mad.lo.u32 %1, %14, %21, %1;\n\t"    \
+    "@pz add.u64 %2, %2, %15;\n\t"            \
+    "@px and.b32 %0, %0, 0xFFFFFFC3;\n\t"     \
+    "@py and.b32 %1, %1, %16;\n\t"            \
+    "@pz and.b64 %2, %2, %17;\n\t"            \
+    "@px add.rn.f32 %3, %3, %10;\n\t"         \
+    "@py add.rn.f32 %4, %4, %11;\n\t"         \
+    "@pz add.rn.f32 %5, %5, %12;\n\t"         \
+    "and.pred q, px, py;\n\t"                 \
+    "and.pred r, px, pz;\n\t"                 \
+    "or.pred q, q, r;\n\t"                    \
+    "and.pred r, py, pz;\n\t"                 \
+    "or.pred q, q, r;\n\t"                    \
+    "mov.f32 %6, m;\n\t"                      \
+    "@q bra VXL_WTIE" #i ";\n"                \
+    "VXL_WBACK" #i ":\n\t"
+#define VXL_LEANW_TIE(i)                      \
+    "VXL_WTIE" #i ":\n\t"                     \
+    "and.pred r, px, py;\n\t"                 \
+    "and.pred r, r, pz;\n\t"                  \
+    "add.rn.f32 b, m, m;\n\t"                 \
+    "@r add.rn.f32 b, b, m;\n\t"              \
+    "@!r add.rn.f32 b, b, 0f00000000;\n\t"    \
+    "setp.lt.f32 pn, b, %19;\n\t"             \
+    "@!pn bra VXL_WEND;\n\t"                  \
+    "mov.f32 %6, b;\n\t"                      \
+    "bra VXL_WBACK" #i ";\n"
+#define VXL_LEANW_IT4(o) VXL_LEANW_IT(o##0) VXL_LEANW_IT(o##1) VXL_LEANW_IT(o##2) VXL_LEANW_IT(o##3)
+#define VXL_LEANW_TIE4(o) VXL_LEANW_TIE(o##0) VXL_LEANW_TIE(o##1) VXL_LEANW_TIE(o##2) VXL_LEANW_TIE(o##3)
+
+// KSTEP = 8 iterations; returns 0 (batch done), 1 (set cell: state of its
+// iteration kept) or 2 (ended by a tie's totalt)
+__device__ __forceinline__ int lean_batch_w(const uint32_t* __restrict__ w, uint32_t& ax, uint32_t& ay, uint64_t& az,
+                                            float& tx, float& ty, float& tz, float tdx, float tdy, float tdz,
+                                            uint32_t kx, uint32_t ky, uint64_t kz, uint32_t keep_y, uint64_t keep_z,
+                                            uint32_t one, float maxt, float& tot, uint32_t& wc, uint32_t& wd) {
+    int stop;
+    uint32_t unused = 0;
+    asm volatile("{\n\t"
+                 ".reg .pred px, py, pz, pb, q, r, pn, pw;\n\t"
+                 ".reg .b32 a, s, zl, zh;\n\t"
+                 ".reg .b64 ad;\n\t"
+                 ".reg .f32 m, b;\n\t" VXL_LEANW_IT4(1) VXL_LEANW_IT4(2)
+                 "mov.u32 %7, 0;\n\t"
+                 "bra VXL_WDONE;\n"
+                 "VXL_WSET:\n\t"
+                 "mov.u32 %7, 1;\n\t"
+                 "bra VXL_WDONE;\n"
+                 "VXL_WEND:\n\t"
+                 "mov.u32 %7, 2;\n\t"
+                 "bra VXL_WDONE;\n" VXL_LEANW_TIE4(1) VXL_LEANW_TIE4(2) "VXL_WDONE:\n\t"
+                 "}"
+                 : "+r"(ax), "+r"(ay), "+l"(az), "+f"(tx), "+f"(ty), "+f"(tz), "+f"(tot), "=r"(stop), "+r"(wc),
+                   "+r"(wd)
+                 : "f"(tdx), "f"(tdy), "f"(tdz), "r"(kx), "r"(ky), "l"(kz), "r"(keep_y), "l"(keep_z), "l"(w),
+                   "f"(maxt), "r"(unused), "r"(one));
+    return stop;
+}
+
+#ifndef VXL_LEANW_MIN_BLOCKS
+#define VXL_LEANW_MIN_BLOCKS 8
+#endif
+
+// lean_tile on the wide layout (KSTEP 8)
+template <int TP>
+__device__ __forceinline__ void lean_tile_w(const SceneDesc& S, const LeanGridW& L, int64_t tile, PSlot* slots,
+                                            float* res_t, uint32_t* res_hit, int lane, uint32_t one) {
+    constexpr int KSTEP = 8;
+    const TraceConstsP& c = S.c;
+    const int R = c.R;
+    const unsigned ux = S.g.ux, uy = S.g.uy, uz = S.g.uz;
+    const uint32_t keep_y = L.keep[1];
+    const uint64_t keep_z = L.keepz;
+    constexpr int LPP = 32 / TP;
+    // ------------------------------------------------ A: generation
+    const int p = lane % TP;
+    int64_t gpix;
+    const bool inimg = tile_pixel<TP>(S, tile, p, &gpix);
+    f3 Pp = mk(0.0f, 0.0f, 0.0f), N = mk(0.0f, 0.0f, 0.0f);
+    float ro = c.default_rough;
+    if (inimg) {
+        Pp = ld3(S.pos + 3 * gpix);
+        N = ld3(S.nrm + 3 * gpix);
+        if (S.rough) ro = S.rough[gpix];
+    }
+    const bool sky = !inimg || (N.x == 0.0f && N.y == 0.0f && N.z == 0.0f);
+    const uint32_t hpix = pcg(c.seed_h + ((uint32_t)gpix + S.pix_base));
+    const f3 O = add(Pp, mul(N, c.bias));
+    f3 T, B;
+    tangent_frame(N, &T, &B);
+    for (int k = lane; k < R; k += 32) res_hit[k] = 0u;
+    int live = 0;
+    const int rounds = (R + LPP - 1) / LPP;
+    for (int j = 0; j < rounds; j++) {
+        const int kk = j * LPP + lane / TP;
+        const int k = !c.spec_first ? kk : (kk < c.n_spec ? c.n_shadow + c.n_ao + kk : kk - c.n_spec);
+        bool is_live = false;
+        PSlot sl;
+        if (kk < R && !sky) {
+            const f3 d = gen_dir(c, k, hpix, Pp, N, T, B, ro);
+            const float maxt = kind_maxt(c, k);
+            const int meta = (p << 4) | (k << 9);
+            if (!ray_domain_ok(O, d)) {
+            } else if (!dir_fast_ok(d)) {
+                is_live = true;
+                sl.c01 = 0;
+                sl.c2m = (meta | kMetaLit) << 16;
+                sl.a0 = O.x; sl.a1 = O.y; sl.a2 = O.z;
+                sl.b0 = d.x; sl.b1 = d.y; sl.b2 = d.z;
+            } else {
+                DState s;
+                dda_init(s, O, d, maxt);
+                if ((unsigned)s.cx <= ux && (unsigned)s.cy <= uy && (unsigned)s.cz <= uz) {
+                    is_live = true;
+                    const int sg = (s.sx < 0 ? 1 : 0) | (s.sy < 0 ? 2 : 0) | (s.sz < 0 ? 4 : 0);
+                    const uint32_t xs = (uint32_t)(s.cx + 4), ys = (uint32_t)(s.cy + 4), zs = (uint32_t)(s.cz + 4);
+                    const uint64_t A = (uint64_t)((xs & 3u) | ((xs >> 2) << L.hs[0]) | ((ys & 3u) << 2) |
+                                                  ((ys >> 2) << L.hs[1]) | ((zs & 3u) << 4)) |
+                                       ((uint64_t)(zs >> 2) << L.hs[2]);
+                    sl.c01 = (int)(uint32_t)A;
+                    sl.c2m = ((meta | sg) << 16) | (int)(A >> 32);
+                    sl.a0 = s.tx; sl.a1 = s.ty; sl.a2 = s.tz;
+                    sl.b0 = s.tdx; sl.b1 = s.tdy; sl.b2 = s.tdz;
+                }
+            }
+        }
+        const unsigned lv = __ballot_sync(0xffffffffu, is_live);
+        if (is_live) slots[live + __popc(lv & lanes_below())] = sl;
+        live += __popc(lv);
+    }
+    __syncwarp();
+
+    // ------------------------------------------------- B: traversal
+    int base = 0;
+    bool busy = false, retired = false;
+    uint32_t ax = 0, ay = 0, kx = 0, ky = 0, wc = 0xffffffffu, wd = 0;
+    uint64_t az = 0, kz = 0;
+    float tx = 0.0f, ty = 0.0f, tz = 0.0f, tdx = 0.0f, tdy = 0.0f, tdz = 0.0f, maxt = 0.0f, tot = 0.0f;
+    int n = 0, meta = 0;
+    for (;;) {
+        const bool need = !busy && !retired;
+        const unsigned nm = __ballot_sync(0xffffffffu, need);
+        if (nm) {
+            if (need) {
+                const int at = base + __popc(nm & lanes_below());
+                if (at < live) {
+                    const PSlot sl = slots[at];
+                    meta = (unsigned)sl.c2m >> 16;
+                    const int k = (meta >> 9) & 31;
+                    maxt = kind_maxt(c, k);
+                    if (meta & kMetaLit) {
+                        const Hit h = dda_literal(S.g, mk(sl.a0, sl.a1, sl.a2), mk(sl.b0, sl.b1, sl.b2), maxt);
+                        if (h.flags & VXL_RF_HIT) {
+                            const int pp = (meta >> 4) & 31;
+                            res_t[k * TP + pp] = h.t;
+                            atomicOr(&res_hit[k], 1u << pp);
+                        }
+                    } else {
+                        busy = true;
+                        const uint64_t A = (uint64_t)(uint32_t)sl.c01 | ((uint64_t)(sl.c2m & 0xffff) << 32);
+                        ax = (uint32_t)A & L.field[0];
+                        ay = (uint32_t)A & L.field[1];
+                        az = A & L.fieldz;
+                        kx = (meta & 1) ? 0u - L.unit[0] : L.inc[0];
+                        ky = (meta & 2) ? 0u - L.unit[1] : L.inc[1];
+                        kz = (meta & 4) ? 0ull - L.unitz : L.incz;
+                        tx = sl.a0; ty = sl.a1; tz = sl.a2;
+                        tdx = sl.b0; tdy = sl.b1; tdz = sl.b2;
+                        tot = -INFINITY;
+                        n = 0;
+                        wc = 0xffffffffu;
+                    }
+                } else {
+                    retired = true;
+                }
+            }
+            base += __popc(nm);
+        }
+        if (!__any_sync(0xffffffffu, busy) && base >= live) break;
+        if (busy) {
+            int res = 0;
+            float ht = 0.0f;
+            if (__all_sync(__activemask(), n + KSTEP <= 256)) {
+                const int st = lean_batch_w(L.w, ax, ay, az, tx, ty, tz, tdx, tdy, tdz, kx, ky, kz, keep_y, keep_z,
+                                            one, maxt, tot, wc, wd);
+                if (st == 1)
+                    res = lean_set_cell_w(L, ax, ay, az, tx, ty, tz, tot, maxt, &ht) ? 1 : 2;
+                else if (st == 2)
+                    res = 2;
+                else {
+                    n += KSTEP;
+                    if (!(tot < maxt)) res = 2;
+                }
+            } else {
+                for (int it = 0; it < KSTEP; it++) {
+                    if (n >= 256) {
+                        res = 2;
+                        break;
+                    }
+                    res = lean_step_w(L, ax, ay, az, tx, ty, tz, tdx, tdy, tdz, kx, ky, kz, maxt, tot, &ht, wc, wd);
+                    if (res) break;
+                    n++;
+                    if (!(tot < maxt) || n >= 256) {
+                        res = 2;
+                        break;
+                    }
+                }
+            }
+            if (res) {
+                if (res == 1) {
+                    const int k = (meta >> 9) & 31, pp = (meta >> 4) & 31;
+                    res_t[k * TP + pp] = ht;
+                    atomicOr(&res_hit[k], 1u << pp);
+                }
+                busy = false;
+            }
+        }
+    }
+    __syncwarp();
+
+    // ------------------------------------------------------ C: fold
+    if (lane < TP && inimg) {
+        float sh = 1.0f, ao = 1.0f, vis = 1.0f, sp = 1.0f, st = c.spec_len;
+        if (!sky) {
+            int k = 0;
+            if (c.n_shadow > 0) {
+                sh = ((res_hit[0] >> p) & 1u) ? 0.0f : 1.0f;
+                k = 1;
+            }
+            float acc = 0.0f, v = 0.0f;
+            for (int j = 0; j < c.n_ao; j++, k++) {
+                const bool hit = (res_hit[k] >> p) & 1u;
+                const float t = res_t[k * TP + p];
+                float tt = hit ? (t < c.ao_len ? t : c.ao_len) : c.ao_len;
+                float q = tt / c.ao_len;
+                acc += q * q;
+                v += hit ? 0.0f : 1.0f;
+            }
+            if (c.n_ao > 0) {
+                ao = acc / (float)c.n_ao;
+                vis = v / (float)c.n_ao;
+            }
+            if (c.n_spec > 0) {
+                float spa = 0.0f, sta = 0.0f;
+                for (int j = 0; j < c.n_spec; j++, k++) {
+                    const bool hit = (res_hit[k] >> p) & 1u;
+                    spa += hit ? 0.0f : 1.0f;
+                    sta += hit ? res_t[k * TP + p] : c.spec_len;
+                }
+                sp = spa / (float)c.n_spec;
+                st = sta / (float)c.n_spec;
+            }
+        }
+        if (S.o_shadow) S.o_shadow[gpix] = sh;
+        if (S.o_ao) S.o_ao[gpix] = ao;
+        if (S.o_vis) S.o_vis[gpix] = vis;
+        if (S.o_spec) S.o_spec[gpix] = sp;
+        if (S.o_spec_t) S.o_spec_t[gpix] = st;
+    }
+    __syncwarp();
+}
+
+template <int TP>
+__global__ void __launch_bounds__(128, VXL_LEANW_MIN_BLOCKS) k_occl_lean_w(const __grid_constant__ LeanSceneW P,
+                                                                           unsigned long long* __restrict__ counter,
+                                                                           int grab) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int R = P.S.c.R;
+    unsigned char* wbase = smem + warp * pool_bytes(TP, R);
+    PSlot* slots = reinterpret_cast<PSlot*>(wbase);
+    float* res_t = reinterpret_cast<float*>(wbase + (size_t)TP * R * sizeof(PSlot));
+    uint32_t* res_hit = reinterpret_cast<uint32_t*>(wbase + (size_t)TP * R * (sizeof(PSlot) + sizeof(float)));
+    for (;;) {
+        int64_t t0 = 0;
+        if (lane == 0) t0 = (int64_t)atomicAdd(counter, (unsigned long long)grab);
+        t0 = __shfl_sync(0xffffffffu, t0, 0);
+        if (t0 >= P.S.ntiles) break;
+        for (int gi = 0; gi < grab && t0 + gi < P.S.ntiles; gi++)
+            lean_tile_w<TP>(P.S, P.L, t0 + gi, slots, res_t, res_hit, lane, P.L.one);
+    }
+}
+
+template <int TP>
+static vxl_status launch_lean_w(vxl_ctx* ctx, const LeanSceneW& P, unsigned long long* counter, int grab,
+                                cudaStream_t s) {
+    const size_t smem = pool_bytes(TP, P.S.c.R) * 4;
+    auto kern = k_occl_lean_w<TP>;
+    VXL_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    VXL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem));
+    if (per_sm < 1) return fail(VXL_ERR_NOT_SUPPORTED, "occlusion pool: %zu bytes of shared memory per block", smem);
+    int64_t blocks = (int64_t)ctx->sm_count * per_sm;
+    const int64_t warps_needed = (P.S.ntiles + grab - 1) / grab;
+    if (blocks * 4 > warps_needed) blocks = (warps_needed + 3) / 4;
+    kern<<<(unsigned)blocks, 128, smem, s>>>(P, counter, grab);
+    ctx->launches++;
+    VXL_TRY_CUDA(cudaGetLastError());
+    return VXL_OK;
+}
+
 bool occl_lean_supported(const vxl_grid* g, const vxl_outputs* out, const vxl_tuning& tune) {
-    return g->tl_words != nullptr && !out->records && tune.leap != 1;
+    // leap 3 (the two-level map of empty space) runs on the exact-step kernel
+    return g->tl_words != nullptr && !out->records && tune.leap != 1 && !(g->tl_wide && tune.leap == 3);
 }
 
 vxl_status launch_trace_occlusion_lean(vxl_ctx* ctx, const vxl_grid* g, const vxl_gbuffer* gb,
@@ -605,6 +1042,16 @@ vxl_status launch_trace_occlusion_lean(vxl_ctx* ctx, const vxl_grid* g, const vx
     if (t.tile_px == 16 && (pool_bytes(16, R) * 4 + 1024) * VXL_LEAN_MIN_BLOCKS > (size_t)ctx->smem_per_sm) {
         t.tile_px = 8;
         t.tile_w = 8;
+    }
+    if (g->tl_wide) {
+        LeanSceneW PW;
+        PW.S = scene_of(g, gb, p, out, t);
+        PW.S.pix_base = pix_base;
+        PW.L = lean_grid_w_of(g);
+        VXL_TRY_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s));
+        if (t.tile_px == 8) return launch_lean_w<8>(ctx, PW, d_counter, t.grab, s);
+        if (t.tile_px == 32) return launch_lean_w<32>(ctx, PW, d_counter, t.grab, s);
+        return launch_lean_w<16>(ctx, PW, d_counter, t.grab, s);
     }
     LeanScene P;
     P.S = scene_of(g, gb, p, out, t);
@@ -620,7 +1067,7 @@ vxl_status launch_trace_occlusion_lean(vxl_ctx* ctx, const vxl_grid* g, const vx
 bool lean_batch_supported(const vxl_batch_item* items, int n, const vxl_tuning& tune) {
     if (tune.leap == 1) return false;
     for (int i = 0; i < n; i++)
-        if (!items[i].grid->tl_words) return false;
+        if (!items[i].grid->tl_words || items[i].grid->tl_wide) return false;
     return true;
 }
 

@@ -346,8 +346,9 @@ vxl_status vxl_grid_create(vxl_ctx* ctx, int nx, int ny, int nz, vxl_grid** out)
     g->nclear2 = ((size_t)g->sx2 * g->sy2 * g->sz2 + 31) / 32;
     cudaError_t e = cudaMalloc(&g->words, g->nwords * sizeof(uint64_t));
     if (e == cudaSuccess) e = cudaMalloc(&g->tmask, g->nmask * sizeof(uint32_t));
-    if (e == cudaSuccess && !g->tl_nwords) e = cudaMalloc(&g->clear1, g->nmask * sizeof(uint32_t));
-    if (e == cudaSuccess && !g->tl_nwords) e = cudaMalloc(&g->clear2, g->nclear2 * sizeof(uint32_t));
+    const bool maps = !g->tl_nwords || g->tl_wide;  // the exact-step kernel's two-level map of empty space
+    if (e == cudaSuccess && maps) e = cudaMalloc(&g->clear1, g->nmask * sizeof(uint32_t));
+    if (e == cudaSuccess && maps) e = cudaMalloc(&g->clear2, g->nclear2 * sizeof(uint32_t));
     if (e == cudaSuccess && g->tl_nwords) e = cudaMalloc(&g->tl_words, g->tl_nwords * sizeof(uint64_t));
     if (e == cudaSuccess) e = cudaMemset(g->words, 0, g->nwords * sizeof(uint64_t));
     if (e == cudaSuccess && g->tl_nwords) e = cudaMemset(g->tl_words, 0, g->tl_nwords * sizeof(uint64_t));
@@ -411,7 +412,7 @@ vxl_status vxl_grid_describe(const vxl_grid* g, vxl_grid_desc* out) {
     out->trace_lbx = g->tl_lbx;
     out->trace_lby = g->tl_lby;
     out->trace_bz = g->tl_bz;
-    out->pad = 0;
+    out->trace_wide = g->tl_wide;
     return VXL_OK;
 }
 

@@ -67,10 +67,14 @@ struct vxl_grid {
     // axis, bricks per x row and per y column padded to powers of two
     // (2^tl_lbx, 2^tl_lby, tl_bz z slabs), and a solid border one cell outside
     // the DDA's inclusive bounds (cells -1 and n+2). Rebuilt from `words` with
-    // the tile map; NULL when the bit addresses would not fit in 32 bits.
+    // the tile map; NULL when the bit addresses would not fit in 37 bits.
     uint64_t* tl_words;
     size_t tl_nwords;
     int tl_lbx, tl_lby, tl_bz;
+    // 1: the bit addresses need more than 32 bits (up to 37: about 2048^3 cells);
+    // the z term then has its brick index above bit 31 and is traced by
+    // k_occl_lean_w
+    int tl_wide;
     // Two-level map of empty space, for grids without a trace layout: level 1
     // is the tile map dilated by one tile (a tile's bit is set when it or one
     // of its 26 neighbours has a voxel), level 2 has one bit per 64^3 cells
