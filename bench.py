@@ -41,6 +41,11 @@ WORKLOADS = {
     # stress: 2048^3 terrain (amplitude 512) + 50,000 instances of edge 16-128, 4K frame
     "c5": dict(kind="terrain", n=2048, W=3840, H=2160, boxes=0, instances=50000, n_shadow=1, n_ao=16, ao_len=64.0,
                n_spec=1, spec_len=256.0, shadow_len=256.0, seed=5, storage="occupancy"),
+    # the stress workload's kernel on a quarter of its area (1024^3 terrain, 12,500 instances, 1920x1080), small
+    # enough for a multi-pass ncu capture (under 1 GB on the device); the grid's bit addresses need 34 bits, so it
+    # takes the same wide trace layout as 2048^3
+    "c5s": dict(kind="terrain", n=1024, W=1920, H=1080, boxes=0, instances=12500, n_shadow=1, n_ao=16, ao_len=64.0,
+                n_spec=1, spec_len=256.0, shadow_len=256.0, seed=5, storage="occupancy"),
 }
 L2_BYTES = 129 * 1024 * 1024
 
