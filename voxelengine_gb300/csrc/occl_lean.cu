@@ -703,14 +703,15 @@ __device__ __forceinline__ bool lean_set_cell_w(const LeanGridW& L, uint32_t ax,
     return true;
 }
 
-// The hot form on the wide layout: the iteration of VXL_LEAN_IT with the x
-// and y adds as multiply-adds by 1, the z term's add and mask in 64 bits, the
-// word index as a funnel shift of the address's two halves, and the load only
-// when that index differs from the cached one.
+// The hot form on the wide layout: the iteration of VXL_LEAN_IT with the
+// adds as multiply-adds by 1 (the z term's as a signed 32-bit step times 1
+// plus the 64-bit term), the z mask on the term's low half (its gap lies
+// below bit 32), the word index as a funnel shift of the address's two
+// halves, and the load only when that index differs from the cached one.
 #define VXL_LEANW_IT(i)                       \
     "mov.b64 {zl, zh}, %2;\n\t"               \
     "mad.lo.u32 a, %0, %21, %1;\n\t"          \
-    "add.u32 a, a, zl;\n\t"                   \
+    "mad.lo.u32 a, zl, %21, a;\n\t"           \
     "shf.r.clamp.b32 s, a, zh, 5;\n\t"        \
     "setp.ne.u32 pw, s, %8;\n\t"              \
     "@pw mad.wide.u32 ad, s, 4, %18;\n\t"     \
@@ -727,10 +728,12 @@ __device__ __forceinline__ bool lean_set_cell_w(const LeanGridW& L, uint32_t ax,
     "@pb bra VXL_WSET;\n\t"                   \
     "@px mad.lo.u32 %0, %13, %21, %0;\n\t"    \
     "@py mad.lo.u32 %1, %14, %21, %1;\n\t"    \
-    "@pz add.u64 %2, %2, %15;\n\t"            \
+    "@pz mad.wide.s32 %2, %15, %21, %2;\n\t"  \
     "@px and.b32 %0, %0, 0xFFFFFFC3;\n\t"     \
     "@py and.b32 %1, %1, %16;\n\t"            \
-    "@pz and.b64 %2, %2, %17;\n\t"            \
+    "mov.b64 {zl, zh}, %2;\n\t"               \
+    "@pz and.b32 zl, zl, %17;\n\t"            \
+    "mov.b64 %2, {zl, zh};\n\t"               \
     "@px add.rn.f32 %3, %3, %10;\n\t"         \
     "@py add.rn.f32 %4, %4, %11;\n\t"         \
     "@pz add.rn.f32 %5, %5, %12;\n\t"         \
@@ -760,7 +763,7 @@ __device__ __forceinline__ bool lean_set_cell_w(const LeanGridW& L, uint32_t ax,
 // iteration kept) or 2 (ended by a tie's totalt)
 __device__ __forceinline__ int lean_batch_w(const uint32_t* __restrict__ w, uint32_t& ax, uint32_t& ay, uint64_t& az,
                                             float& tx, float& ty, float& tz, float tdx, float tdy, float tdz,
-                                            uint32_t kx, uint32_t ky, uint64_t kz, uint32_t keep_y, uint64_t keep_z,
+                                            uint32_t kx, uint32_t ky, int32_t kz, uint32_t keep_y, uint32_t keep_z,
                                             uint32_t one, float maxt, float& tot, uint32_t& wc, uint32_t& wd) {
     int stop;
     uint32_t unused = 0;
@@ -780,7 +783,7 @@ __device__ __forceinline__ int lean_batch_w(const uint32_t* __restrict__ w, uint
                  "}"
                  : "+r"(ax), "+r"(ay), "+l"(az), "+f"(tx), "+f"(ty), "+f"(tz), "+f"(tot), "=r"(stop), "+r"(wc),
                    "+r"(wd)
-                 : "f"(tdx), "f"(tdy), "f"(tdz), "r"(kx), "r"(ky), "l"(kz), "r"(keep_y), "l"(keep_z), "l"(w),
+                 : "f"(tdx), "f"(tdy), "f"(tdz), "r"(kx), "r"(ky), "r"(kz), "r"(keep_y), "r"(keep_z), "l"(w),
                    "f"(maxt), "r"(unused), "r"(one));
     return stop;
 }
@@ -798,7 +801,7 @@ __device__ __forceinline__ void lean_tile_w(const SceneDesc& S, const LeanGridW&
     const int R = c.R;
     const unsigned ux = S.g.ux, uy = S.g.uy, uz = S.g.uz;
     const uint32_t keep_y = L.keep[1];
-    const uint64_t keep_z = L.keepz;
+    const uint32_t keep_z = (uint32_t)L.keepz;  // the z gap lies below bit 32: the high half of the mask is all ones
     constexpr int LPP = 32 / TP;
     // ------------------------------------------------ A: generation
     const int p = lane % TP;
@@ -909,8 +912,8 @@ __device__ __forceinline__ void lean_tile_w(const SceneDesc& S, const LeanGridW&
             int res = 0;
             float ht = 0.0f;
             if (__all_sync(__activemask(), n + KSTEP <= 256)) {
-                const int st = lean_batch_w(L.w, ax, ay, az, tx, ty, tz, tdx, tdy, tdz, kx, ky, kz, keep_y, keep_z,
-                                            one, maxt, tot, wc, wd);
+                const int st = lean_batch_w(L.w, ax, ay, az, tx, ty, tz, tdx, tdy, tdz, kx, ky, (int32_t)kz, keep_y,
+                                            keep_z, one, maxt, tot, wc, wd);
                 if (st == 1)
                     res = lean_set_cell_w(L, ax, ay, az, tx, ty, tz, tot, maxt, &ht) ? 1 : 2;
                 else if (st == 2)
