@@ -127,7 +127,9 @@ vxl_status vxl_ctx_get_tuning(const vxl_ctx* ctx, vxl_tuning* out);
  * needs no bounds test: the first cell outside the bounds reads as set, and
  * is reported as the bounds exit. Present when every bit address fits in 37
  * bits (trace_words != NULL; up to about 2048^3 cells), trace_wide = 1 when
- * they need more than 32; rebuilt with the tile map. */
+ * they need more than 32 (such a layout takes about 4x the grid's words,
+ * 4.3 GB at 2048^3; where it cannot be allocated the grid has none and is
+ * traced on its own words); rebuilt with the tile map. */
 typedef struct vxl_grid_desc {
     int32_t nx, ny, nz;        /* fine dimensions */
     int32_t bx, by, bz;        /* 4^3 bricks per axis, padding included */

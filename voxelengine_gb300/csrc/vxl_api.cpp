@@ -349,7 +349,18 @@ vxl_status vxl_grid_create(vxl_ctx* ctx, int nx, int ny, int nz, vxl_grid** out)
     const bool maps = !g->tl_nwords || g->tl_wide;  // the exact-step kernel's two-level map of empty space
     if (e == cudaSuccess && maps) e = cudaMalloc(&g->clear1, g->nmask * sizeof(uint32_t));
     if (e == cudaSuccess && maps) e = cudaMalloc(&g->clear2, g->nclear2 * sizeof(uint32_t));
-    if (e == cudaSuccess && g->tl_nwords) e = cudaMalloc(&g->tl_words, g->tl_nwords * sizeof(uint64_t));
+    if (e == cudaSuccess && g->tl_nwords) {
+        e = cudaMalloc(&g->tl_words, g->tl_nwords * sizeof(uint64_t));
+        if (e == cudaErrorMemoryAllocation && g->tl_wide) {
+            // the wide layout is 4x the grid's own words (4.3 GB at 2048^3): without room for it the grid is
+            // traced on its own words by the exact-step kernel, whose maps are allocated above
+            (void)cudaGetLastError();
+            g->tl_words = nullptr;
+            g->tl_nwords = 0;
+            g->tl_wide = 0;
+            e = cudaSuccess;
+        }
+    }
     if (e == cudaSuccess) e = cudaMemset(g->words, 0, g->nwords * sizeof(uint64_t));
     if (e == cudaSuccess && g->tl_nwords) e = cudaMemset(g->tl_words, 0, g->tl_nwords * sizeof(uint64_t));
     if (e != cudaSuccess) {
