@@ -95,7 +95,8 @@ vxl_status vxl_ctx_launch_count(const vxl_ctx* ctx, uint64_t* out);
  * (voxelengine_gb300/autotune.py). */
 typedef struct vxl_tuning {
     int32_t tile_px;   /* pixels per warp tile: 8, 16 or 32 (the exact-step and batched kernels run 8 as 16) */
-    int32_t kstep;     /* DDA iterations between pool refills: 1, 2, 4 or 8 */
+    int32_t kstep;     /* DDA iterations between pool refills: 1, 2, 4, 8 or 16 (16: the single-scene
+                          trace-layout kernel; the others run 8 for it) */
     int32_t leap;      /* empty-space skipping: 1 = cross empty bricks in one step where exact; 2 = none;
                           3 = on grids without a trace layout (its bit addresses would not fit in 32 bits: about
                           1000^3 cells and up), end a ray once its remaining path is proved empty on the two-level

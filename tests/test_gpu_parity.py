@@ -87,9 +87,11 @@ def test_gbuffer_matches_oracle(vxl, ctx):
     assert (np.abs(n2).sum(1) > 0).mean() > 0.3  # the camera sees mostly geometry
 
 
-@pytest.mark.parametrize("n_spec", [0, 1])
-def test_occlusion_c1_bit_exact(vxl, ctx, n_spec):
-    """C1: 256^3 noise grid, 640x360 G-buffer, 1 shadow + 4 AO (L=16) [+ 1 GGX spec]."""
+@pytest.mark.parametrize("n_spec,kstep", [(0, 0), (1, 0), (1, 4), (1, 16)])
+def test_occlusion_c1_bit_exact(vxl, ctx, n_spec, kstep):
+    """C1: 256^3 noise grid, 640x360 G-buffer, 1 shadow + 4 AO (L=16) [+ 1 GGX spec];
+    the trace-layout kernel also with batches of 4 and 16 DDA iterations
+    (tuning kstep; 0 = the default 8)."""
     import torch
 
     G, cam, tgt, pos, nrm, rough = _c1_scene(vxl, ctx)
@@ -106,10 +108,16 @@ def test_occlusion_c1_bit_exact(vxl, ctx, n_spec):
     assert_recs_equal(recs_np(rec), want["recs"], "records")
     for k in outs:
         assert same_bits(outs[k].cpu().numpy(), want[k]).all(), k
-    # without records: same buffers
+    # without records (the trace-layout kernel): same buffers
     outs2 = {k: empty(npix, torch.float32) for k in outs}
-    vxl.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, **outs2)
-    torch.cuda.synchronize()
+    before = ctx.get_tuning()
+    try:
+        if kstep:
+            ctx.set_tuning(kstep=kstep)
+        vxl.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, **outs2)
+        torch.cuda.synchronize()
+    finally:
+        ctx.set_tuning(**before)
     for k in outs:
         assert torch.equal(outs[k], outs2[k]), k
 

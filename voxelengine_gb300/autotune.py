@@ -21,7 +21,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CACHE = os.path.join(HERE, "tuning_cache.json")
 
 SHAPES = [(16, 16), (16, 8), (16, 4), (32, 32), (32, 8)]  # (tile_px, tile_w)
-KSTEPS = [2, 4, 8]
+KSTEPS = [2, 4, 8, 16]
 GRABS = [1, 2, 4]
 ORDERS = [1, 2]
 

@@ -215,10 +215,13 @@ __device__ __forceinline__ int lean_batch(const uint32_t* __restrict__ w, uint32
                                           float& tx, float& ty, float& tz, float tdx, float tdy, float tdz,
                                           uint32_t kx, uint32_t ky, uint32_t kz, uint32_t keep_y, uint32_t keep_z,
                                           uint32_t one, uint32_t two27, float maxt, float& tot) {
-    static_assert(KSTEP == 4 || KSTEP == 8, "batch of 4 or 8 iterations");
+    static_assert(KSTEP == 4 || KSTEP == 8 || KSTEP == 16, "batch of 4, 8 or 16 iterations");
     int stop;
     if (KSTEP == 4) VXL_LEAN_BLOCK(VXL_LEAN_IT4(1), VXL_LEAN_TIE4(1));
     if (KSTEP == 8) VXL_LEAN_BLOCK(VXL_LEAN_IT4(1) VXL_LEAN_IT4(2), VXL_LEAN_TIE4(1) VXL_LEAN_TIE4(2));
+    if (KSTEP == 16)
+        VXL_LEAN_BLOCK(VXL_LEAN_IT4(1) VXL_LEAN_IT4(2) VXL_LEAN_IT4(3) VXL_LEAN_IT4(4),
+                       VXL_LEAN_TIE4(1) VXL_LEAN_TIE4(2) VXL_LEAN_TIE4(3) VXL_LEAN_TIE4(4));
     return stop;
 }
 
@@ -587,6 +590,7 @@ static vxl_status launch_lean_k(vxl_ctx* ctx, const LeanScene& P, unsigned long 
         case 1:
         case 2:
         case 4: return launch_lean_t<TP, 4>(ctx, P, counter, t.grab, s);
+        case 16: return launch_lean_t<TP, 16>(ctx, P, counter, t.grab, s);
         default: return launch_lean_t<TP, 8>(ctx, P, counter, t.grab, s);
     }
 }

@@ -390,6 +390,7 @@ bool occl_pool_supported(const vxl_grid* g, const vxl_trace_params* p) {
 // chosen below for many rays per pixel); an 8-pixel tuning runs as 16
 static vxl_tuning pool_tuning(const vxl_tuning& t) {
     vxl_tuning r = t;
+    if (r.kstep == 16) r.kstep = 8;  // 16-iteration batches exist in the trace-layout kernel only
     if (r.tile_px == 8) {
         r.tile_px = 16;
         if (r.tile_w == 8) r.tile_w = 16;

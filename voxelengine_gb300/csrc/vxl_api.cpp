@@ -281,8 +281,8 @@ vxl_status vxl_ctx_set_tuning(vxl_ctx* ctx, const vxl_tuning* t) {
         n.tile_px = t->tile_px;
     }
     if (t->kstep) {
-        if (t->kstep != 1 && t->kstep != 2 && t->kstep != 4 && t->kstep != 8)
-            return fail(VXL_ERR_INVALID_ARG, "kstep must be 1, 2, 4 or 8");
+        if (t->kstep != 1 && t->kstep != 2 && t->kstep != 4 && t->kstep != 8 && t->kstep != 16)
+            return fail(VXL_ERR_INVALID_ARG, "kstep must be 1, 2, 4, 8 or 16");
         n.kstep = t->kstep;
     }
     if (t->leap) {
