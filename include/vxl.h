@@ -34,7 +34,8 @@
  *      - vxl_trace_primary reads its tile-list total back to the host;
  *      - the voxelizer calls upload host tables and wait for them;
  *      - vxl_trace_occlusion_host and vxl_grid_count are synchronous;
- *      - the create and destroy calls allocate or free.
+ *      - the create and destroy calls, and vxl_grid_palette_alloc, allocate or
+ *        free.
  *    A captured call fixes its scalar arguments and pointers in the graph,
  *    and replays of one graph must not overlap.
  */
