@@ -122,6 +122,34 @@ def test_occlusion_c1_bit_exact(vxl, ctx, n_spec, kstep):
         assert torch.equal(outs[k], outs2[k]), k
 
 
+@pytest.mark.parametrize("light", [(0.0, 0.8, 0.6), (0.0, 1.0, 0.0)])
+def test_occlusion_literal_rays_bit_exact(vxl, ctx, light):
+    """Shadow rays whose direction has zero components take the literal
+    4-pass form of raycastShadowVolume (Light.frag:29-81), traced after the
+    trace-layout kernel's stepping loop: C1 scene, outputs and records equal
+    to the oracle, and the same buffers without records."""
+    import torch
+
+    G, cam, tgt, pos, nrm, rough = _c1_scene(vxl, ctx)
+    npix = 640 * 360
+    kw = dict(light_dir=light, cam_pos=cam, n_ao=4, ao_len=16.0, n_spec=1, seed=7)
+    P = vxl.make_params(**kw)
+    outs = {k: empty(npix, torch.float32) for k in ("shadow", "ao", "ao_vis", "spec", "spec_t")}
+    rec = rec_buffer(npix * 6)
+    vxl.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, records=rec, **outs)
+    outs2 = {k: empty(npix, torch.float32) for k in outs}
+    vxl.trace_occlusion(ctx, G, pos, nrm, rough, npix, P, width=640, height=360, **outs2)
+    torch.cuda.synchronize()
+    want = oracle.occlusion(export_r8(G), pos.cpu().numpy(), nrm.cpu().numpy(), rough.cpu().numpy(),
+                            oracle.make_params(**kw), with_recs=True)
+    assert_recs_equal(recs_np(rec), want["recs"], "records")
+    for k in outs:
+        assert same_bits(outs[k].cpu().numpy(), want[k]).all(), k
+        assert torch.equal(outs[k], outs2[k]), k
+    # (with a zero direction component the reference's t_max for that axis is 0/0 or x/0, and its loop
+    # reports no hit: every shadow ray is lit, here as in the oracle)
+
+
 @pytest.mark.parametrize("scene,ao_len,shadow_len", [("boxes", 32.0, 100.0), ("boxes", 64.0, 130.0),
                                                      ("noise", 24.0, 60.0)])
 def test_occlusion_leap_matches_exact(vxl, ctx, scene, ao_len, shadow_len):

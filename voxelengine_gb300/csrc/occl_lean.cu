@@ -258,12 +258,12 @@ __device__ __forceinline__ void lean_tile(const SceneDesc& S, const LeanGrid& L,
     f3 T, B;
     tangent_frame(N, &T, &B);
     for (int k = lane; k < R; k += 32) res_hit[k] = 0u;
-    int live = 0;
+    int live = 0, nlit = 0;
     const int rounds = (R + LPP - 1) / LPP;
     for (int j = 0; j < rounds; j++) {
         const int kk = j * LPP + lane / TP;
         const int k = !c.spec_first ? kk : (kk < c.n_spec ? c.n_shadow + c.n_ao + kk : kk - c.n_spec);
-        bool is_live = false;
+        bool is_live = false, is_lit = false;
         PSlot sl;
         if (kk < R && !sky) {
             const f3 d = gen_dir(c, k, hpix, Pp, N, T, B, ro);
@@ -272,7 +272,7 @@ __device__ __forceinline__ void lean_tile(const SceneDesc& S, const LeanGrid& L,
             if (!ray_domain_ok(O, d)) {
                 // no traversal: a miss
             } else if (!dir_fast_ok(d)) {
-                is_live = true;
+                is_lit = true;
                 sl.c01 = 0;
                 sl.c2m = (meta | kMetaLit) << 16;
                 sl.a0 = O.x; sl.a1 = O.y; sl.a2 = O.z;
@@ -296,6 +296,13 @@ __device__ __forceinline__ void lean_tile(const SceneDesc& S, const LeanGrid& L,
         const unsigned lv = __ballot_sync(0xffffffffu, is_live);
         if (is_live) slots[live + __popc(lv & lanes_below())] = sl;
         live += __popc(lv);
+        // rays with a direction component below 1e-30 take the literal form of the DDA after the
+        // traversal loop (no call inside it): their slots fill the pool from its top down
+        const unsigned lm = __ballot_sync(0xffffffffu, is_lit);
+        if (lm) {
+            if (is_lit) slots[TP * R - 1 - (nlit + __popc(lm & lanes_below()))] = sl;
+            nlit += __popc(lm);
+        }
     }
     __syncwarp();
 
@@ -316,14 +323,7 @@ __device__ __forceinline__ void lean_tile(const SceneDesc& S, const LeanGrid& L,
                     meta = (unsigned)sl.c2m >> 16;
                     const int k = (meta >> 9) & 31;
                     maxt = kind_maxt(c, k);
-                    if (meta & kMetaLit) {
-                        const Hit h = dda_literal(S.g, mk(sl.a0, sl.a1, sl.a2), mk(sl.b0, sl.b1, sl.b2), maxt);
-                        if (h.flags & VXL_RF_HIT) {
-                            const int pp = (meta >> 4) & 31;
-                            res_t[k * TP + pp] = h.t;
-                            atomicOr(&res_hit[k], 1u << pp);
-                        }
-                    } else {
+                    {
                         busy = true;
                         const uint32_t A = (uint32_t)sl.c01;
                         ax = A & L.field[0];
@@ -382,6 +382,16 @@ __device__ __forceinline__ void lean_tile(const SceneDesc& S, const LeanGrid& L,
                 }
                 busy = false;
             }
+        }
+    }
+    for (int i = lane; i < nlit; i += 32) {
+        const PSlot sl = slots[TP * R - 1 - i];
+        const int m = (unsigned)sl.c2m >> 16, k = (m >> 9) & 31;
+        const Hit h = dda_literal(S.g, mk(sl.a0, sl.a1, sl.a2), mk(sl.b0, sl.b1, sl.b2), kind_maxt(c, k));
+        if (h.flags & VXL_RF_HIT) {
+            const int pp = (m >> 4) & 31;
+            res_t[k * TP + pp] = h.t;
+            atomicOr(&res_hit[k], 1u << pp);
         }
     }
     __syncwarp();
@@ -824,12 +834,12 @@ __device__ __forceinline__ void lean_tile_w(const SceneDesc& S, const LeanGridW&
     f3 T, B;
     tangent_frame(N, &T, &B);
     for (int k = lane; k < R; k += 32) res_hit[k] = 0u;
-    int live = 0;
+    int live = 0, nlit = 0;
     const int rounds = (R + LPP - 1) / LPP;
     for (int j = 0; j < rounds; j++) {
         const int kk = j * LPP + lane / TP;
         const int k = !c.spec_first ? kk : (kk < c.n_spec ? c.n_shadow + c.n_ao + kk : kk - c.n_spec);
-        bool is_live = false;
+        bool is_live = false, is_lit = false;
         PSlot sl;
         if (kk < R && !sky) {
             const f3 d = gen_dir(c, k, hpix, Pp, N, T, B, ro);
@@ -837,7 +847,7 @@ __device__ __forceinline__ void lean_tile_w(const SceneDesc& S, const LeanGridW&
             const int meta = (p << 4) | (k << 9);
             if (!ray_domain_ok(O, d)) {
             } else if (!dir_fast_ok(d)) {
-                is_live = true;
+                is_lit = true;
                 sl.c01 = 0;
                 sl.c2m = (meta | kMetaLit) << 16;
                 sl.a0 = O.x; sl.a1 = O.y; sl.a2 = O.z;
@@ -862,6 +872,13 @@ __device__ __forceinline__ void lean_tile_w(const SceneDesc& S, const LeanGridW&
         const unsigned lv = __ballot_sync(0xffffffffu, is_live);
         if (is_live) slots[live + __popc(lv & lanes_below())] = sl;
         live += __popc(lv);
+        // rays with a direction component below 1e-30 take the literal form of the DDA after the
+        // traversal loop (no call inside it): their slots fill the pool from its top down
+        const unsigned lm = __ballot_sync(0xffffffffu, is_lit);
+        if (lm) {
+            if (is_lit) slots[TP * R - 1 - (nlit + __popc(lm & lanes_below()))] = sl;
+            nlit += __popc(lm);
+        }
     }
     __syncwarp();
 
@@ -883,14 +900,7 @@ __device__ __forceinline__ void lean_tile_w(const SceneDesc& S, const LeanGridW&
                     meta = (unsigned)sl.c2m >> 16;
                     const int k = (meta >> 9) & 31;
                     maxt = kind_maxt(c, k);
-                    if (meta & kMetaLit) {
-                        const Hit h = dda_literal(S.g, mk(sl.a0, sl.a1, sl.a2), mk(sl.b0, sl.b1, sl.b2), maxt);
-                        if (h.flags & VXL_RF_HIT) {
-                            const int pp = (meta >> 4) & 31;
-                            res_t[k * TP + pp] = h.t;
-                            atomicOr(&res_hit[k], 1u << pp);
-                        }
-                    } else {
+                    {
                         busy = true;
                         const uint64_t A = (uint64_t)(uint32_t)sl.c01 | ((uint64_t)(sl.c2m & 0xffff) << 32);
                         ax = (uint32_t)A & L.field[0];
@@ -949,6 +959,16 @@ __device__ __forceinline__ void lean_tile_w(const SceneDesc& S, const LeanGridW&
                 }
                 busy = false;
             }
+        }
+    }
+    for (int i = lane; i < nlit; i += 32) {
+        const PSlot sl = slots[TP * R - 1 - i];
+        const int m = (unsigned)sl.c2m >> 16, k = (m >> 9) & 31;
+        const Hit h = dda_literal(S.g, mk(sl.a0, sl.a1, sl.a2), mk(sl.b0, sl.b1, sl.b2), kind_maxt(c, k));
+        if (h.flags & VXL_RF_HIT) {
+            const int pp = (m >> 4) & 31;
+            res_t[k * TP + pp] = h.t;
+            atomicOr(&res_hit[k], 1u << pp);
         }
     }
     __syncwarp();
