@@ -802,8 +802,10 @@ __device__ __forceinline__ int lean_batch_w(const uint32_t* __restrict__ w, uint
     return stop;
 }
 
+// 9 blocks per SM (56 registers): 2.4% faster on the 2048^3 stress frame than
+// 8 at 64, whose 8-pixel pools (18 rays per pixel) leave room for a ninth
 #ifndef VXL_LEANW_MIN_BLOCKS
-#define VXL_LEANW_MIN_BLOCKS 8
+#define VXL_LEANW_MIN_BLOCKS 9
 #endif
 
 // lean_tile on the wide layout (KSTEP 8)
