@@ -128,10 +128,11 @@ vxl_status vxl_ctx_get_tuning(const vxl_ctx* ctx, vxl_tuning* out);
  * outside those bounds (a coordinate equal to -1 or n+2). The traversal then
  * needs no bounds test: the first cell outside the bounds reads as set, and
  * is reported as the bounds exit. Present when every bit address fits in 37
- * bits (trace_words != NULL; up to about 2048^3 cells), trace_wide = 1 when
- * they need more than 32 (such a layout takes about 4x the grid's words,
- * 4.3 GB at 2048^3; where it cannot be allocated the grid has none and is
- * traced on its own words); rebuilt with the tile map. */
+ * bits (trace_words != NULL; cubic grids up to about 4000^3 cells),
+ * trace_wide = 1 when they need more than 32 (cubic grids from about 1020^3;
+ * such a layout takes about 4x the grid's words, 4.3 GB at 2048^3; where it
+ * cannot be allocated the grid has none and is traced on its own words);
+ * rebuilt with the tile map. */
 typedef struct vxl_grid_desc {
     int32_t nx, ny, nz;        /* fine dimensions */
     int32_t bx, by, bz;        /* 4^3 bricks per axis, padding included */

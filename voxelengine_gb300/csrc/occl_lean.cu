@@ -606,8 +606,9 @@ static vxl_status launch_lean_k(vxl_ctx* ctx, const LeanScene& P, unsigned long 
 }
 
 // ------------------------------------------------------ wide trace layout
-// Grids whose bit addresses need 33 to 37 bits (about 1300^3 to 2048^3
-// cells): the x and y terms stay 32-bit, the z term is 64-bit (its brick
+// Grids whose bit addresses need 33 to 37 bits (cubic grids from about 1020^3
+// cells, where a row passes 256 bricks; 2048^3 needs 35): the x and y terms
+// stay 32-bit, the z term is 64-bit (its brick
 // index lies above bit 31), and a cell's 32-bit word index is the 64-bit
 // address >> 5. Such a grid does not stay in L1 the way a 512^3 one does, so
 // each ray keeps the word it last read and loads only when its word index
