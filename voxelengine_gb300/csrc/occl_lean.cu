@@ -774,7 +774,21 @@ __device__ __forceinline__ bool lean_set_cell_w(const LeanGridW& L, uint32_t ax,
 #define VXL_LEANW_IT4(o) VXL_LEANW_IT(o##0) VXL_LEANW_IT(o##1) VXL_LEANW_IT(o##2) VXL_LEANW_IT(o##3)
 #define VXL_LEANW_TIE4(o) VXL_LEANW_TIE(o##0) VXL_LEANW_TIE(o##1) VXL_LEANW_TIE(o##2) VXL_LEANW_TIE(o##3)
 
-// KSTEP = 8 iterations; returns 0 (batch done), 1 (set cell: state of its
+// 16 iterations per batch: the stress frame's rays are long (57 reference
+// steps on average), so half the batch ends cost less than the lane slots
+// idle after a ray ends (1.1% faster than 8 on C5)
+#ifndef VXL_LEANW_KSTEP
+#define VXL_LEANW_KSTEP 16
+#endif
+#if VXL_LEANW_KSTEP == 16
+#define VXL_LEANW_ITERS VXL_LEANW_IT4(1) VXL_LEANW_IT4(2) VXL_LEANW_IT4(3) VXL_LEANW_IT4(4)
+#define VXL_LEANW_TIES VXL_LEANW_TIE4(1) VXL_LEANW_TIE4(2) VXL_LEANW_TIE4(3) VXL_LEANW_TIE4(4)
+#else
+#define VXL_LEANW_ITERS VXL_LEANW_IT4(1) VXL_LEANW_IT4(2)
+#define VXL_LEANW_TIES VXL_LEANW_TIE4(1) VXL_LEANW_TIE4(2)
+#endif
+
+// VXL_LEANW_KSTEP iterations; returns 0 (batch done), 1 (set cell: state of its
 // iteration kept) or 2 (ended by a tie's totalt)
 __device__ __forceinline__ int lean_batch_w(const uint32_t* __restrict__ w, uint32_t& ax, uint32_t& ay, uint64_t& az,
                                             float& tx, float& ty, float& tz, float tdx, float tdy, float tdz,
@@ -786,7 +800,7 @@ __device__ __forceinline__ int lean_batch_w(const uint32_t* __restrict__ w, uint
                  ".reg .pred px, py, pz, pb, q, r, pn, pw;\n\t"
                  ".reg .b32 a, s, zl, zh;\n\t"
                  ".reg .b64 ad;\n\t"
-                 ".reg .f32 m, b;\n\t" VXL_LEANW_IT4(1) VXL_LEANW_IT4(2)
+                 ".reg .f32 m, b;\n\t" VXL_LEANW_ITERS
                  "mov.u32 %7, 0;\n\t"
                  "bra VXL_WDONE;\n"
                  "VXL_WSET:\n\t"
@@ -794,7 +808,7 @@ __device__ __forceinline__ int lean_batch_w(const uint32_t* __restrict__ w, uint
                  "bra VXL_WDONE;\n"
                  "VXL_WEND:\n\t"
                  "mov.u32 %7, 2;\n\t"
-                 "bra VXL_WDONE;\n" VXL_LEANW_TIE4(1) VXL_LEANW_TIE4(2) "VXL_WDONE:\n\t"
+                 "bra VXL_WDONE;\n" VXL_LEANW_TIES "VXL_WDONE:\n\t"
                  "}"
                  : "+r"(ax), "+r"(ay), "+l"(az), "+f"(tx), "+f"(ty), "+f"(tz), "+f"(tot), "=r"(stop), "+r"(wc),
                    "+r"(wd)
@@ -813,7 +827,7 @@ __device__ __forceinline__ int lean_batch_w(const uint32_t* __restrict__ w, uint
 template <int TP>
 __device__ __forceinline__ void lean_tile_w(const SceneDesc& S, const LeanGridW& L, int64_t tile, PSlot* slots,
                                             float* res_t, uint32_t* res_hit, int lane, uint32_t one) {
-    constexpr int KSTEP = 8;
+    constexpr int KSTEP = VXL_LEANW_KSTEP;
     const TraceConstsP& c = S.c;
     const int R = c.R;
     const unsigned ux = S.g.ux, uy = S.g.uy, uz = S.g.uz;
